@@ -1,0 +1,500 @@
+// gbstencil engine: the C ABI of include/gbstencil.h.
+//
+// Replaces the AN5D-generated host sequencer of every benchmark
+// (compiled/<prec>/<cfg>_host.cu:10-566: cudaMalloc, H2D of both planes, a
+// loop of ceil(T/bt) launches with parity-correcting remainder launches, D2H,
+// cudaFree) with a planner that picks the fused degree and tiling per grid,
+// a launch sequence whose final plane is T%2 by construction, host-side
+// validation of every address range a launch touches, and status codes in
+// place of asserts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gbstencil.h"
+#include "engine_internal.h"
+#include "stencil_defs.h"
+
+namespace gbs {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+gbs_status fail(gbs_status st, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return st;
+}
+
+gbs_status cuda_fail(cudaError_t e, const char *what) {
+  if (e == cudaErrorMemoryAllocation)
+    return fail(GBS_ERR_NOMEM, "%s: %s", what, cudaGetErrorString(e));
+  return fail(GBS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// launcher registry (the instantiation units)
+// ---------------------------------------------------------------------------
+#define GBS_DECL(id, S)                 \
+  Picks picks_##id##_f_e();             \
+  Picks picks_##id##_f_m();             \
+  Picks picks_##id##_d_e();             \
+  Picks picks_##id##_d_m();
+GBS_FOR_EACH_STENCIL(GBS_DECL)
+#undef GBS_DECL
+
+static const Picks &picks(int sid, int dtype, int fma) {
+  static std::once_flag once;
+  static Picks table[kNumStencils][2][2];
+  std::call_once(once, [] {
+#define GBS_FILL(id, S)                     \
+  table[id][0][0] = picks_##id##_f_e();     \
+  table[id][0][1] = picks_##id##_f_m();     \
+  table[id][1][0] = picks_##id##_d_e();     \
+  table[id][1][1] = picks_##id##_d_m();
+    GBS_FOR_EACH_STENCIL(GBS_FILL)
+#undef GBS_FILL
+  });
+  return table[sid][dtype][fma];
+}
+
+int max_bt(int sid, int dtype, int fma) {
+  const Picks &p = picks(sid, dtype, fma);
+  return p.ncls ? p.cls[p.ncls - 1] : 0;
+}
+
+// ---------------------------------------------------------------------------
+// descriptors and layout
+// ---------------------------------------------------------------------------
+const gbs_stencil_def_t *stencil_def(int sid) {
+  if (sid < 0 || sid >= GBS_NUM_STENCILS) return nullptr;
+  return &gbs_stencil_defs[sid];
+}
+
+gbs_status check_desc(const gbs_desc *d) {
+  if (!d) return fail(GBS_ERR_INVALID, "descriptor is NULL");
+  const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  if (!s) return fail(GBS_ERR_INVALID, "unknown stencil id %d", d->stencil);
+  if (d->dtype != GBS_F32 && d->dtype != GBS_F64)
+    return fail(GBS_ERR_INVALID, "dtype must be GBS_F32 or GBS_F64 (got %d)", d->dtype);
+  if (d->fp_mode != GBS_FP_EXACT && d->fp_mode != GBS_FP_FMA)
+    return fail(GBS_ERR_INVALID, "fp_mode must be GBS_FP_EXACT or GBS_FP_FMA (got %d)", d->fp_mode);
+  for (int a = 0; a < s->dim; ++a)
+    if (d->n[a] < 1 || d->n[a] > (1 << 24))
+      return fail(GBS_ERR_INVALID, "interior extent n[%d]=%d out of range [1, 2^24]", a, d->n[a]);
+  if (d->timestep < 0) return fail(GBS_ERR_INVALID, "timestep must be >= 0 (got %d)", d->timestep);
+  if (d->bt < 0 || d->sl < 0 || d->bs1 < 0 || d->bs2 < 0)
+    return fail(GBS_ERR_INVALID, "bt/bs1/bs2/sl must be >= 0");
+  return GBS_OK;
+}
+
+size_t elem_size(int dtype) { return dtype == GBS_F64 ? 8 : 4; }
+
+Layout make_layout(const gbs_desc *d) {
+  const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  Layout L{};
+  L.dim = s->dim;
+  L.rad = s->rad;
+  L.esize = elem_size(d->dtype);
+  L.V = (int)(16 / L.esize);
+  for (int a = 0; a < 3; ++a) L.dims[a] = a < s->dim ? d->n[a] + 2 * s->rad : 1;
+  const int inner = L.dims[s->dim - 1];
+  // column c at element shift + c; the first interior column is 16-byte aligned
+  L.shift = (L.V - s->rad % L.V) % L.V;
+  // every 32*V-element window starting at an aligned element < shift + inner
+  // must fit in the row
+  const long long need = (long long)L.shift + inner + 32 * L.V;
+  const long long align = 128 / (long long)L.esize;
+  L.pitch = (need + align - 1) / align * align;
+  L.rows = s->dim == 2 ? (long long)L.dims[0] : (long long)L.dims[0] * L.dims[1];
+  L.plane = L.rows * L.pitch;
+  L.bytes = 2ull * (size_t)L.plane * L.esize;
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// planning
+// ---------------------------------------------------------------------------
+static int default_bt(const gbs_desc *d) {
+  const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  const int mx = max_bt(d->stencil, d->dtype, d->fp_mode);
+  if (d->dtype == GBS_F64) return 1;
+  int bt = 1;
+  if (s->dim == 2) {
+    if (s->kind == 1) bt = d->fp_mode == GBS_FP_FMA ? 4 : 1;
+    else if (s->fpp <= 20) bt = 8 / (s->rad > 1 ? 2 : 1);
+    else if (s->fpp <= 40) bt = 2;
+    else bt = 1;
+  }
+  return std::max(1, std::min(bt, mx));
+}
+
+// splits T steps into n launches of at most bt steps with n == T (mod 2), so
+// that launch j reads plane j%2 and the result lands in plane T%2.
+std::vector<int> split_steps(int T, int bt) {
+  std::vector<int> out;
+  if (T <= 0) return out;
+  int n = (T + bt - 1) / bt;
+  if ((n - T) % 2 != 0) ++n;
+  const int q = T / n, rem = T % n;
+  for (int j = 0; j < n; ++j) out.push_back(q + (j < rem ? 1 : 0));
+  return out;
+}
+
+Geometry2D geometry2d(const Layout &L, int b, int sl_req, int sid) {
+  Geometry2D g{};
+  const int R = L.rad, V = L.V;
+  g.b = b;
+  g.wout = ((32 * V - 2 * b * R - (V - 1)) / V) * V;
+  const int ni = L.dims[0] - 2 * R, nj = L.dims[1] - 2 * R;
+  g.nstrips = (nj + g.wout - 1) / g.wout;
+  int sl = sl_req;
+  if (sl <= 0) {
+    // about two waves of 16 warps per SM over 152 SMs, but blocks at least
+    // 8*b*r rows long so that the stream overlap stays small
+    const long long target = 152LL * 16 * 2;
+    long long nb = std::max<long long>(1, target / std::max(1, g.nstrips));
+    sl = (int)((ni + nb - 1) / nb);
+    sl = std::max(sl, std::max(16, 8 * b * R));
+  }
+  g.sl = std::min(sl, ni);
+  g.nblocks = (ni + g.sl - 1) / g.sl;
+  (void)sid;
+  return g;
+}
+
+// Every address range a 2-D launch touches, checked against the buffer.
+gbs_status validate2d(const Layout &L, const Geometry2D &g) {
+  const int R = L.rad, V = L.V, ROW = 32 * V;
+  if (g.wout <= 0) return fail(GBS_ERR_UNSUPPORTED, "fused degree %d leaves no output columns", g.b);
+  if (L.shift % 1 != 0 || (L.pitch * (long long)L.esize) % 16 != 0)
+    return fail(GBS_ERR_INVALID, "internal: row pitch not 16-byte aligned");
+  for (int s = 0; s < g.nstrips; ++s) {
+    const int cs = R + s * g.wout;
+    const int ce = std::min(cs + g.wout, L.dims[1] - R);
+    const int need_lo = std::max(0, cs - g.b * R);
+    const int need_hi = std::min(L.dims[1], ce + g.b * R);
+    const long long ws = ((need_lo + L.shift) / V) * (long long)V;
+    if (ws < 0 || ws + ROW > L.pitch)
+      return fail(GBS_ERR_INVALID, "internal: strip %d window [%lld,%lld) outside row of %lld", s, ws,
+                  ws + ROW, L.pitch);
+    if (need_hi + L.shift > ws + ROW)
+      return fail(GBS_ERR_INVALID, "internal: strip %d window misses columns", s);
+    if ((ws * (long long)L.esize) % 16 != 0) return fail(GBS_ERR_INVALID, "internal: unaligned window");
+  }
+  return GBS_OK;
+}
+
+}  // namespace gbs
+
+using namespace gbs;
+
+// ---------------------------------------------------------------------------
+// device state: error word, cached buffer, stream
+// ---------------------------------------------------------------------------
+namespace {
+struct DeviceState {
+  int *err = nullptr;          // error word of the kernels (device)
+  void *buf = nullptr;         // gbs_run's cached grid buffer
+  size_t buf_bytes = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+std::mutex g_mu;
+DeviceState g_dev[64];
+
+gbs_status device_state(DeviceState **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(GBS_ERR_NODEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return fail(GBS_ERR_NODEVICE, "device ordinal %d unsupported", dev);
+  DeviceState &s = g_dev[dev];
+  if (!s.err) {
+    if ((e = cudaMalloc(&s.err, sizeof(int))) != cudaSuccess) return cuda_fail(e, "cudaMalloc(error word)");
+    if ((e = cudaMemset(s.err, 0, sizeof(int))) != cudaSuccess) return cuda_fail(e, "cudaMemset");
+  }
+  *out = &s;
+  return GBS_OK;
+}
+}  // namespace
+
+namespace gbs {
+gbs_status error_word(int **out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState *s;
+  gbs_status st = device_state(&s);
+  if (st != GBS_OK) return st;
+  *out = s->err;
+  return GBS_OK;
+}
+
+// Enqueues the whole time loop of `d` on `stream` for a buffer in layout L.
+gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_t stream, int *err) {
+  const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
+  const Picks &pk = picks(d->stencil, d->dtype, fma);
+  if (pk.ncls == 0)
+    return fail(GBS_ERR_UNSUPPORTED, "no kernels built for %s dtype=%d fp_mode=%d", s->name, d->dtype,
+                d->fp_mode);
+  int bt = d->bt > 0 ? d->bt : default_bt(d);
+  if (bt > pk.cls[pk.ncls - 1])
+    return fail(GBS_ERR_UNSUPPORTED, "bt=%d exceeds the largest fused degree built for %s (%d)", bt,
+                s->name, pk.cls[pk.ncls - 1]);
+  // coefficients
+  std::vector<double> coef(s->nterms > 0 ? s->nterms : 1);
+  if (s->kind == 1) {
+    coef[0] = d->coef ? (d->dtype == GBS_F64 ? ((const double *)d->coef)[0] : ((const float *)d->coef)[0])
+                      : (double)s->numerator;
+  } else {
+    for (int t = 0; t < s->nterms; ++t)
+      coef[t] = d->coef ? (d->dtype == GBS_F64 ? ((const double *)d->coef)[t] : ((const float *)d->coef)[t])
+                        : (double)s->terms[t].coef;
+  }
+  const double div = d->divisor != 0.0 ? d->divisor : (double)s->divisor;
+  const double eps = d->eps != 0.0 ? d->eps : (double)s->eps;
+  if (s->divisor && div == 0.0) return fail(GBS_ERR_INVALID, "divisor must be nonzero");
+
+  const std::vector<int> steps = split_steps(d->timestep, bt);
+  char *base = static_cast<char *>(dev_A);
+  const size_t plane_bytes = (size_t)L.plane * L.esize;
+  for (size_t j = 0; j < steps.size(); ++j) {
+    const int b = steps[j];
+    int c = 0;
+    while (pk.cls[c] < b) ++c;
+    const void *src = base + (j % 2) * plane_bytes;
+    void *dst = base + ((j + 1) % 2) * plane_bytes;
+    if (s->dim == 2) {
+      Geometry2D g = geometry2d(L, b, d->sl, d->stencil);
+      gbs_status st = validate2d(L, g);
+      if (st != GBS_OK) return st;
+      Launch2D a{};
+      a.src = src;
+      a.dst = dst;
+      a.err = err;
+      a.pitch = L.pitch;
+      a.d0 = L.dims[0];
+      a.d1 = L.dims[1];
+      a.shift = L.shift;
+      a.b = b;
+      a.wout = g.wout;
+      a.nstrips = g.nstrips;
+      a.nblocks = g.nblocks;
+      a.sl = g.sl;
+      a.coef = coef.data();
+      a.div = div;
+      a.eps = eps;
+      cudaError_t e = pk.l2[c](a, stream);
+      if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");
+    } else {
+      return fail(GBS_ERR_UNSUPPORTED, "3-D stencils are not built in this configuration");
+    }
+  }
+  return GBS_OK;
+}
+}  // namespace gbs
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int gbs_num_stencils(void) { return GBS_NUM_STENCILS; }
+
+const char *gbs_stencil_name(int id) {
+  const gbs_stencil_def_t *s = stencil_def(id);
+  return s ? s->name : nullptr;
+}
+
+int gbs_stencil_id(const char *name) {
+  if (!name) return -1;
+  for (int i = 0; i < GBS_NUM_STENCILS; ++i)
+    if (std::strcmp(gbs_stencil_defs[i].name, name) == 0) return i;
+  return -1;
+}
+
+gbs_status gbs_stencil_info(int id, int *dim, int *rad, int *nterms, int *fpp) {
+  const gbs_stencil_def_t *s = stencil_def(id);
+  if (!s) return fail(GBS_ERR_INVALID, "unknown stencil id %d", id);
+  if (dim) *dim = s->dim;
+  if (rad) *rad = s->rad;
+  if (nterms) *nterms = s->kind == 1 ? 1 : s->nterms;
+  if (fpp) *fpp = s->fpp;
+  return GBS_OK;
+}
+
+const char *gbs_last_error(void) { return g_last_error.c_str(); }
+
+gbs_status gbs_get_layout(const gbs_desc *d, gbs_layout *out) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!out) return fail(GBS_ERR_INVALID, "out is NULL");
+  const Layout L = make_layout(d);
+  out->pitch = (size_t)L.pitch;
+  out->shift = (size_t)L.shift;
+  out->rows = (size_t)L.rows;
+  out->plane = (size_t)L.plane;
+  out->bytes = L.bytes;
+  for (int a = 0; a < 3; ++a) out->dimsize[a] = L.dims[a];
+  out->dim = L.dim;
+  out->rad = L.rad;
+  return GBS_OK;
+}
+
+gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!out) return fail(GBS_ERR_INVALID, "out is NULL");
+  const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  const Layout L = make_layout(d);
+  const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
+  const int mx = max_bt(d->stencil, d->dtype, fma);
+  if (mx == 0) return fail(GBS_ERR_UNSUPPORTED, "no kernels built for %s", s->name);
+  const int bt = d->bt > 0 ? d->bt : default_bt(d);
+  if (bt > mx) return fail(GBS_ERR_UNSUPPORTED, "bt=%d exceeds the largest fused degree built (%d)", bt, mx);
+  std::memset(out, 0, sizeof *out);
+  out->bt = bt;
+  out->launches = (int)split_steps(d->timestep, bt).size();
+  if (s->dim == 2) {
+    Geometry2D g = geometry2d(L, bt, d->sl, d->stencil);
+    st = validate2d(L, g);
+    if (st != GBS_OK) return st;
+    out->bs1 = 4;
+    out->sl = g.sl;
+    out->ctas = (g.nstrips * g.nblocks + 3) / 4;
+    out->valid_w = g.wout;
+    const double cols = 32.0 * L.V, rows = g.sl + 2.0 * bt * L.rad;
+    out->redundancy = (cols * rows) / ((double)g.wout * g.sl);
+  }
+  return GBS_OK;
+}
+
+gbs_status gbs_upload(const gbs_desc *d, const void *host_A, void *dev_A, void *stream) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!host_A || !dev_A) return fail(GBS_ERR_INVALID, "NULL buffer");
+  const Layout L = make_layout(d);
+  const size_t w = (size_t)L.dims[L.dim - 1] * L.esize;
+  const size_t nrows = 2 * (size_t)L.rows;
+  cudaError_t e = cudaMemcpy2DAsync(static_cast<char *>(dev_A) + L.shift * L.esize, L.pitch * L.esize,
+                                    host_A, w, w, nrows, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "upload");
+  return GBS_OK;
+}
+
+gbs_status gbs_download(const gbs_desc *d, const void *dev_A, void *host_A, void *stream) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!host_A || !dev_A) return fail(GBS_ERR_INVALID, "NULL buffer");
+  const Layout L = make_layout(d);
+  const size_t w = (size_t)L.dims[L.dim - 1] * L.esize;
+  const size_t nrows = 2 * (size_t)L.rows;
+  cudaError_t e = cudaMemcpy2DAsync(host_A, w, static_cast<const char *>(dev_A) + L.shift * L.esize,
+                                    L.pitch * L.esize, w, nrows, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "download");
+  return GBS_OK;
+}
+
+gbs_status gbs_sync(void *stream) {
+  int *err = nullptr;
+  gbs_status st = error_word(&err);
+  if (st != GBS_OK) return st;
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
+  int h = 0;
+  e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read error word");
+  if (h != 0) {
+    cudaMemset(err, 0, sizeof(int));
+    return fail(GBS_ERR_TIMEOUT, "a device-side wait gave up (error bits 0x%x)", h);
+  }
+  return GBS_OK;
+}
+
+gbs_status gbs_run_device(const gbs_desc *d, void *dev_A, void *stream) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!dev_A) return fail(GBS_ERR_INVALID, "dev_A is NULL");
+  if (reinterpret_cast<uintptr_t>(dev_A) % 128 != 0)
+    return fail(GBS_ERR_INVALID, "dev_A must be 128-byte aligned");
+  int *err = nullptr;
+  st = error_word(&err);
+  if (st != GBS_OK) return st;
+  const Layout L = make_layout(d);
+  return run_loop(d, L, dev_A, (cudaStream_t)stream, err);
+}
+
+gbs_status gbs_run(const gbs_desc *d, void *host_A, double *ms_out) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!host_A) return fail(GBS_ERR_INVALID, "host_A is NULL");
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState *s;
+  st = device_state(&s);
+  if (st != GBS_OK) return st;
+  cudaError_t e;
+  if (!s->stream) {
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+      return cuda_fail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreate(&s->ev0)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&s->ev1)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+  }
+  const Layout L = make_layout(d);
+  if (s->buf_bytes < L.bytes) {
+    if (s->buf) cudaFree(s->buf);
+    s->buf = nullptr;
+    s->buf_bytes = 0;
+    if ((e = cudaMalloc(&s->buf, L.bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(grid)");
+    s->buf_bytes = L.bytes;
+    // margins are never part of a result but are read by edge windows
+    if ((e = cudaMemset(s->buf, 0, L.bytes)) != cudaSuccess) return cuda_fail(e, "cudaMemset(grid)");
+  }
+  if ((st = gbs_upload(d, host_A, s->buf, s->stream)) != GBS_OK) return st;
+  if ((e = cudaEventRecord(s->ev0, s->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+  st = run_loop(d, L, s->buf, s->stream, s->err);
+  if (st != GBS_OK) {
+    cudaStreamSynchronize(s->stream);
+    return st;
+  }
+  if ((e = cudaEventRecord(s->ev1, s->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+  if ((st = gbs_download(d, s->buf, host_A, s->stream)) != GBS_OK) return st;
+  {
+    // gbs_sync takes the lock through error_word(); read the word directly
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
+    int h = 0;
+    if ((e = cudaMemcpy(&h, s->err, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return cuda_fail(e, "read error word");
+    if (h != 0) {
+      cudaMemset(s->err, 0, sizeof(int));
+      return fail(GBS_ERR_TIMEOUT, "a device-side wait gave up (error bits 0x%x)", h);
+    }
+  }
+  if (ms_out) {
+    float ms = 0.f;
+    if ((e = cudaEventElapsedTime(&ms, s->ev0, s->ev1)) != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime");
+    *ms_out = ms;
+  }
+  return GBS_OK;
+}
+
+void gbs_release_cache(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto &s : g_dev) {
+    if (s.buf) cudaFree(s.buf);
+    s.buf = nullptr;
+    s.buf_bytes = 0;
+  }
+}
+
+}  // extern "C"

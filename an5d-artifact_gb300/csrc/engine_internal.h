@@ -1,0 +1,42 @@
+// Engine internals shared by the host-side translation units.
+#pragma once
+#include <cstdarg>
+#include <cstddef>
+#include <vector>
+
+#include "../../include/gbstencil.h"
+#include "gbs_launch.h"
+#include "stencil_defs.h"
+#include "stencil_table.cuh"
+
+namespace gbs {
+
+// Device layout of a two-plane grid (see gbs_layout in gbstencil.h).
+struct Layout {
+  int dim, rad, V;
+  size_t esize;
+  int dims[3];          // dimsize per axis
+  long long shift;      // element offset of column 0
+  long long pitch;      // elements per padded innermost row
+  long long rows;       // rows per plane
+  long long plane;      // elements per plane
+  size_t bytes;         // both planes
+};
+
+struct Geometry2D {
+  int b, wout, nstrips, nblocks, sl;
+};
+
+gbs_status fail(gbs_status st, const char *fmt, ...);
+gbs_status cuda_fail(cudaError_t e, const char *what);
+const gbs_stencil_def_t *stencil_def(int sid);
+gbs_status check_desc(const gbs_desc *d);
+Layout make_layout(const gbs_desc *d);
+std::vector<int> split_steps(int T, int bt);
+Geometry2D geometry2d(const Layout &L, int b, int sl_req, int sid);
+gbs_status validate2d(const Layout &L, const Geometry2D &g);
+gbs_status error_word(int **out);
+gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_t stream, int *err);
+int max_bt(int sid, int dtype, int fma);
+
+}  // namespace gbs

@@ -1,0 +1,48 @@
+// Host-side launch descriptions and the per-(stencil, type, mode) launcher
+// tables that the instantiation units export to the engine.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace gbs {
+
+// One launch of the 2-D family (see kernel2d.cuh for the decomposition).
+struct Launch2D {
+  const void *src;
+  void *dst;
+  int *err;
+  long long pitch;
+  int d0, d1, shift, b, wout, nstrips, nblocks, sl;
+  const double *coef;
+  double div, eps;
+};
+
+// One launch of the 3-D family (see kernel3d.cuh).
+struct Launch3D {
+  const void *src;
+  void *dst;
+  int *err;
+  const void *tmap;   // device copy of the level-0 tensor map (64-byte aligned)
+  long long pitch;    // elements per padded k-row
+  int d0, d1, d2, shift, b;
+  int tj, wk;         // tile rows (warps) and valid k columns per tile
+  int jout;           // valid j rows per tile
+  int ntk, ntj, nblocks, sl;
+  int src_plane;      // plane index the tensor map reads
+  const double *coef;
+  double div, eps;
+};
+
+using Launch2DFn = cudaError_t (*)(const Launch2D &, cudaStream_t);
+using Launch3DFn = cudaError_t (*)(const Launch3D &, cudaStream_t);
+
+// Launchers of one (stencil, element type, fp mode): one per fused-degree
+// class; class c handles any b <= cls[c].
+struct Picks {
+  int ncls;
+  int cls[4];
+  Launch2DFn l2[4];
+  Launch3DFn l3[4];
+  int smem3[4];       // dynamic shared memory of the 3-D launchers (bytes)
+};
+
+}  // namespace gbs

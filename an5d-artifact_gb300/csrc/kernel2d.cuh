@@ -1,0 +1,357 @@
+// 2-D temporally-blocked stencil kernel family (sm_103a).
+//
+// Replaces the AN5D-generated 2-D kernels kernel0_<b> (e.g.
+// compiled/float/star2d1r-256-10-256_kernel.cu:4..3488) and computes what
+// the artifact's scop loop computes (star2d1r.c:14-24 and the other 2-D
+// sources): b Jacobi steps of A[(t+1)%2][i][j] = f(A[t%2][neighbourhood]) on
+// the interior, the halo held fixed.
+//
+// Work decomposition. One WARP is the unit of work; warps never wait on each
+// other. A warp owns a strip of output columns [cs, ce) (wout wide) and a
+// block of output rows [i0, i1) (sl long). It streams level-0 rows
+// i0-b*r .. i1-1+b*r through a per-warp ring of NSTAGE shared-memory row
+// buffers filled by bulk-async (TMA) copies, one 32*V-element window row per
+// copy (V = 16 bytes / element size, 512 bytes per copy). Lane l holds window
+// elements [l*V, l*V+V).
+//
+// Per fused time level l (1..b) the warp keeps a (2r+1)-row register window.
+// At pipeline step p (level-0 row p arrives) level l produces row p - l*r,
+// which feeds level l+1 in the same step; level b's row p - b*r is stored if
+// it lies in [i0, i1). Row neighbours at other column offsets come from the
+// neighbouring lanes by shuffles. The window's edge lanes (b*r columns at
+// each side) lose accuracy level by level; they are the overlap that
+// neighbouring strips compute for real (overlapped tiling), so no warp ever
+// needs another warp's result.
+//
+// Two evaluation forms, chosen per stencil by the tap-table generator:
+//  * direct: the window holds the input rows; each output is one chain over
+//    the terms in source order. Used for stars, gradient2d and star2d4r.
+//  * assoc:  the window holds partial sums of the 2r+1 outputs in flight;
+//    each arriving row adds its terms to every output it touches. Used for
+//    stencils whose source groups the terms by ascending row (the boxes,
+//    j2d9pt-gol), where the partial sums are built in exactly the source
+//    order, so both forms give the same bits.
+//
+// Halo cells (rows/columns within r of the grid edge) carry their input
+// value through every level, like the reference's untouched halo.
+#pragma once
+#include "gbs_device.cuh"
+#include "gbs_launch.h"
+#include "stencil_table.cuh"
+
+namespace gbs {
+
+template <typename T, int NT> struct Params2D {
+  const T *src;        // plane read (row 0, element 0 of the padded row)
+  T *dst;              // plane written
+  int *err;            // error word (bounded waits)
+  long long pitch;     // elements per padded row
+  int d0, d1;          // dimsize: rows, columns (interior + 2r)
+  int shift;           // column c is stored at element shift + c
+  int b;               // time levels fused in this launch (1..BTMAX)
+  int wout;            // output columns per strip (multiple of V)
+  int nstrips, nblocks, sl;
+  T coef[NT];
+  T div, eps;
+};
+
+// Compile-time facts about a stencil's term list.
+template <class ST, int V> struct Tap2 {
+  static constexpr int R = ST::kRad;
+  static constexpr int NT = ST::kTerms;
+  // does some term read row offset di at element x (x relative to the lane's
+  // first element, x in [-R, V+R))?
+  __host__ __device__ static constexpr bool need(int di, int x) {
+    if (ST::kKind == KIND_GRADIENT && di == 0 && x >= 0 && x < V) return true;
+    for (int t = 0; t < NT; ++t)
+      if (ST::kOff[t][0] == di) {
+        const int e = x - ST::kOff[t][1];
+        if (e >= 0 && e < V) return true;
+      }
+    return false;
+  }
+  __host__ __device__ static constexpr bool row_has_dj(int di) {
+    for (int t = 0; t < NT; ++t)
+      if (ST::kOff[t][0] == di && ST::kOff[t][1] != 0) return true;
+    if (ST::kKind == KIND_GRADIENT) return false;
+    return false;
+  }
+};
+
+// ext[R + x] = row element x, x in [-R, V+R), for the x some term needs.
+template <class ST, int V, int DI, typename T>
+__device__ __forceinline__ void extend_row(T (&ext)[V + 2 * ST::kRad], const T (&row)[V]) {
+  constexpr int R = ST::kRad;
+  static_for<V + 2 * R>([&](auto XI) {
+    constexpr int x = decltype(XI)::value - R;
+    if constexpr (Tap2<ST, V>::need(DI, x)) ext[R + x] = row_elem<V, x>(row);
+  });
+}
+
+// Window slots: with UNR the loop over pipeline steps is unrolled W times and
+// the logical window position j (0 = oldest row) of phase ph lives in slot
+// (ph + 1 + j) % W, so the window rotates by renaming; without UNR (large
+// radii, to keep the code small) slot == j and the window shifts by moves.
+template <bool UNR, int W>
+__host__ __device__ constexpr int wslot(int ph, int j) { return UNR ? (ph + 1 + j) % W : j; }
+
+template <class ST, typename T, int BTMAX, bool FMA, int WPC, int NSTAGE>
+__global__ void __launch_bounds__(WPC * 32)
+    stencil2d_kernel(const __grid_constant__ Params2D<T, ST::kTerms> p) {
+  constexpr int V = 16 / sizeof(T);
+  constexpr int R = ST::kRad;
+  constexpr int W = 2 * R + 1;
+  constexpr bool UNR = (R <= 2);
+  constexpr int NPH = UNR ? W : 1;
+  constexpr int ROW = 32 * V;
+  constexpr unsigned ROW_BYTES = ROW * sizeof(T);
+  using A = Arith<T>;
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  const long long gw = (long long)blockIdx.x * WPC + wid;
+  if (gw >= (long long)p.nstrips * p.nblocks) return;
+  const int strip = (int)(gw % p.nstrips);
+  const int blk = (int)(gw / p.nstrips);
+  const int b = p.b;
+
+  // ---- columns (column space c; offset space c + shift) ----
+  const int cs = R + strip * p.wout;
+  const int ce = min(cs + p.wout, p.d1 - R);
+  const int need_lo = max(0, cs - b * R);
+  const int ws = ((need_lo + p.shift) / V) * V;
+  const int col0 = ws - p.shift + lane * V;  // column of this lane's element 0
+  const bool edge = (ws - p.shift < R) || (ws - p.shift + ROW > p.d1 - R);
+
+  // ---- rows ----
+  const int i0 = R + blk * p.sl;
+  const int i1 = min(i0 + p.sl, p.d0 - R);
+  const int pstart = max(0, i0 - b * R);
+  const int pend = min(p.d0, i1 + b * R);  // rows loaded: [pstart, pend)
+  const int plast = i1 - 1 + b * R;        // last pipeline step
+  const int nload = pend - pstart;
+
+  T *ring = reinterpret_cast<T *>(smem_raw) + (size_t)wid * NSTAGE * ROW;
+  uint64_t *bars =
+      reinterpret_cast<uint64_t *>(smem_raw + (size_t)WPC * NSTAGE * ROW_BYTES) + wid * NSTAGE;
+  const T *src_win = p.src + ws;
+
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+#pragma unroll 1
+    for (int s = 0; s < NSTAGE && s < nload; ++s) {
+      mbar_arrive_expect_tx(&bars[s], ROW_BYTES);
+      bulk_g2s(ring + s * ROW, src_win + (long long)(pstart + s) * p.pitch, ROW_BYTES, &bars[s]);
+    }
+  }
+  __syncwarp();
+
+  T win[BTMAX][W][V];
+#pragma unroll
+  for (int l = 0; l < BTMAX; ++l)
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+#pragma unroll
+      for (int e = 0; e < V; ++e) win[l][w][e] = T(0);
+
+  int consumed = 0;  // loads consumed so far (for the drain on timeout)
+  bool ok = true;
+
+#pragma unroll 1
+  for (int pb = pstart; pb <= plast && ok; pb += NPH) {
+    static_for<NPH>([&](auto PH) {
+      constexpr int ph = decltype(PH)::value;
+      const int pp = pb + ph;
+      if (!ok || pp > plast) return;
+
+      // ---- level 0: row pp from the ring ----
+      T x[V];
+      if (pp < pend) {
+        const int n = pp - pstart;
+        const int s = n % NSTAGE;
+        // every lane waits; the decision to give up is warp-uniform
+        const bool got = mbar_wait(&bars[s], (unsigned)(n / NSTAGE) & 1u, nullptr, 0);
+        if (!__all_sync(0xffffffffu, got)) {
+          if (lane == 0) atomicOr(p.err, ERR_WAIT_TIMEOUT);
+          ok = false;
+          return;
+        }
+        ld_vec<T, V>(x, ring + s * ROW + lane * V);
+        consumed = n + 1;
+        __syncwarp();
+        if (lane == 0 && n + NSTAGE < nload) {
+          mbar_arrive_expect_tx(&bars[s], ROW_BYTES);
+          bulk_g2s(ring + s * ROW, src_win + (long long)(pp + NSTAGE) * p.pitch, ROW_BYTES,
+                   &bars[s]);
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) x[e] = T(0);
+      }
+
+      // ---- fused time levels ----
+      static_for<BTMAX>([&](auto LI) {
+        constexpr int l = decltype(LI)::value;
+        if (l >= b) return;
+        const int q = pp - (l + 1) * R;  // row produced by level l+1
+        const bool halo_row = (q < R) || (q >= p.d0 - R);
+        T y[V];
+        if constexpr (!ST::kAssoc) {
+          // direct: push the new row, evaluate the centre row q
+#pragma unroll
+          for (int e = 0; e < V; ++e) win[l][wslot<UNR, W>(ph, 2 * R)][e] = x[e];
+          constexpr int cslot = wslot<UNR, W>(ph, R);
+          if (halo_row) {
+#pragma unroll
+            for (int e = 0; e < V; ++e) y[e] = win[l][cslot][e];
+          } else {
+            if constexpr (ST::kKind == KIND_GRADIENT) {
+              T ext[V + 2 * R];
+              extend_row<ST, V, 0>(ext, win[l][cslot]);
+              static_for<V>([&](auto EI) {
+                constexpr int e = decltype(EI)::value;
+                T nb[ST::kTerms];
+                static_for<ST::kTerms>([&](auto TI) {
+                  constexpr int t = decltype(TI)::value;
+                  constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+                  if constexpr (di == 0) nb[t] = ext[R + e + dj];
+                  else nb[t] = win[l][wslot<UNR, W>(ph, R + di)][e];
+                });
+                y[e] = gradient_update<T, FMA, ST::kTerms>(win[l][cslot][e], nb, p.eps, p.coef[0]);
+              });
+            } else {
+              // rows with off-centre columns get their lane-extended copy once
+              T ext[W][V + 2 * R];
+              static_for<W>([&](auto DI) {
+                constexpr int di = decltype(DI)::value - R;
+                if constexpr (Tap2<ST, V>::row_has_dj(di))
+                  extend_row<ST, V, di>(ext[di + R], win[l][wslot<UNR, W>(ph, R + di)]);
+              });
+              static_for<ST::kTerms>([&](auto TI) {
+                constexpr int t = decltype(TI)::value;
+                constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+                constexpr int slot = wslot<UNR, W>(ph, R + di);
+#pragma unroll
+                for (int e = 0; e < V; ++e) {
+                  const T a = (dj == 0) ? win[l][slot][e] : ext[di + R][R + e + dj];
+                  if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
+                  else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
+                }
+              });
+              if constexpr (ST::kHasDiv) {
+#pragma unroll
+                for (int e = 0; e < V; ++e) y[e] = A::div(y[e], p.div);
+              }
+            }
+            if (edge) {
+#pragma unroll
+              for (int e = 0; e < V; ++e)
+                if (col0 + e < R || col0 + e >= p.d1 - R) y[e] = win[l][cslot][e];
+            }
+          }
+        } else {
+          // assoc: the arriving row m = q + R adds its terms to outputs q..q+2R
+          T ext[V + 2 * R];
+          static_for<V + 2 * R>([&](auto XI) {
+            constexpr int xx = decltype(XI)::value - R;
+            bool any = false;
+            static_for<W>([&](auto DI) {
+              constexpr int di = decltype(DI)::value - R;
+              if constexpr (Tap2<ST, V>::need(di, xx)) any = true;
+            });
+            if (any) ext[R + xx] = row_elem<V, xx>(x);
+          });
+          static_for<ST::kTerms>([&](auto TI) {
+            constexpr int t = decltype(TI)::value;
+            constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+            constexpr int slot = wslot<UNR, W>(ph, R - di);
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+              const T a = ext[R + e + dj];
+              if constexpr (t == 0) win[l][slot][e] = A::mul(p.coef[t], a);
+              else win[l][slot][e] = term_next<T, FMA>(win[l][slot][e], p.coef[t], a);
+            }
+          });
+          constexpr int oslot = wslot<UNR, W>(ph, 0);
+#pragma unroll
+          for (int e = 0; e < V; ++e) y[e] = win[l][oslot][e];
+          if constexpr (ST::kHasDiv) {
+#pragma unroll
+            for (int e = 0; e < V; ++e) y[e] = A::div(y[e], p.div);
+          }
+          if (halo_row) {
+            if (q >= 0 && q < p.d0) ld_vec_global<T, V>(y, p.src + (long long)q * p.pitch + ws + lane * V);
+          } else if (edge) {
+            T c[V];
+            ld_vec_global<T, V>(c, p.src + (long long)q * p.pitch + ws + lane * V);
+#pragma unroll
+            for (int e = 0; e < V; ++e)
+              if (col0 + e < R || col0 + e >= p.d1 - R) y[e] = c[e];
+          }
+        }
+        if constexpr (!UNR) {
+#pragma unroll
+          for (int j = 0; j < 2 * R; ++j)
+#pragma unroll
+            for (int e = 0; e < V; ++e) win[l][j][e] = win[l][j + 1][e];
+        }
+#pragma unroll
+        for (int e = 0; e < V; ++e) x[e] = y[e];
+      });
+
+      // ---- store level b's row ----
+      const int q = pp - b * R;
+      if (q >= i0 && q < i1) {
+        T *d = p.dst + (long long)q * p.pitch + ws + lane * V;
+        if (col0 >= cs && col0 + V <= ce) {
+          st_vec<T, V>(d, x);
+        } else {
+#pragma unroll
+          for (int e = 0; e < V; ++e)
+            if (col0 + e >= cs && col0 + e < ce) d[e] = x[e];
+        }
+      }
+    });
+  }
+
+  if (!ok && lane == 0) {
+    // Timed out: wait (bounded) for the copies still in flight into this
+    // warp's ring before the CTA may exit and release its shared memory.
+    const int issued = min(nload, consumed + NSTAGE);
+    for (int n = consumed; n < issued; ++n)
+      if (!mbar_wait(&bars[n % NSTAGE], (unsigned)(n / NSTAGE) & 1u, p.err, ERR_DRAIN_TIMEOUT)) break;
+  }
+}
+
+template <class ST, typename T, int BTMAX, bool FMA>
+cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
+  constexpr int WPC = 4, NSTAGE = 8;
+  constexpr int V = 16 / sizeof(T);
+  Params2D<T, ST::kTerms> p;
+  p.src = static_cast<const T *>(a.src);
+  p.dst = static_cast<T *>(a.dst);
+  p.err = a.err;
+  p.pitch = a.pitch;
+  p.d0 = a.d0;
+  p.d1 = a.d1;
+  p.shift = a.shift;
+  p.b = a.b;
+  p.wout = a.wout;
+  p.nstrips = a.nstrips;
+  p.nblocks = a.nblocks;
+  p.sl = a.sl;
+  for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = (T)a.coef[t];
+  p.div = (T)a.div;
+  p.eps = (T)a.eps;
+  const size_t smem = (size_t)WPC * NSTAGE * (32 * V * sizeof(T) + sizeof(uint64_t));
+  const long long warps = (long long)a.nstrips * a.nblocks;
+  const long long grid = (warps + WPC - 1) / WPC;
+  stencil2d_kernel<ST, T, BTMAX, FMA, WPC, NSTAGE><<<(unsigned)grid, WPC * 32, smem, stream>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace gbs

@@ -1,0 +1,142 @@
+/* gbstencil: GB300-native temporally-blocked stencil engine, C ABI.
+ *
+ * This is the drop-in boundary for the AN5D artifact's per-benchmark stencil
+ * time loop. Every benchmark there defines
+ *
+ *     double kernel_stencil(SB_TYPE *A1, int compsize, int timestep, bool scop);
+ *
+ * (declared at common.h:42, defined at <stencil>.c:7 and, in generated form,
+ * at compiled/<prec>/<cfg>_host.cu:10). Its scop==true branch is the GPU time
+ * loop that gbs_run() replaces; the artifact's C harness (common.h: main,
+ * -s/-t/-n/-c, init_grid, check_result) stays as it is.
+ *
+ * Grid convention (the reference's): a grid of interior extent n[] per axis
+ * is stored with a fixed Dirichlet halo of width r, so dimsize = n + 2r per
+ * axis, and two time planes: A[2][d0][d1] (2-D) or A[2][d0][d1][d2] (3-D),
+ * row-major, last index fastest. Step t reads plane t%2 and writes the
+ * interior of plane (t+1)%2; the halo is never written. After T steps plane
+ * T%2 holds u_T. Halo cells must hold the same values in both planes (as
+ * init_grid, common.h:50-55, sets them).
+ *
+ * No function here allocates on the caller's behalf except gbs_run (which,
+ * like the reference's host code, owns its device copy) and the batch /
+ * adjoint planners, which say so. All functions return a gbs_status; none
+ * aborts. gbs_last_error() describes the last failure of the calling thread.
+ */
+#ifndef GBSTENCIL_H
+#define GBSTENCIL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gbs_status {
+  GBS_OK = 0,
+  GBS_ERR_INVALID = 1,     /* bad descriptor or argument */
+  GBS_ERR_UNSUPPORTED = 2, /* no kernel instantiated for this combination */
+  GBS_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  GBS_ERR_NOMEM = 4,       /* a device or pinned-host allocation failed */
+  GBS_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  GBS_ERR_NODEVICE = 6     /* no usable sm_103 device */
+} gbs_status;
+
+enum { GBS_F32 = 0, GBS_F64 = 1 };
+
+/* Floating-point evaluation mode.
+ * GBS_FP_EXACT: every product and sum rounded separately, in the order the
+ *   artifact's source writes the terms; divisions and square roots IEEE. The
+ *   result is bit-identical to the artifact's CPU path (kernel_stencil with
+ *   scop==false) built without floating-point contraction.
+ * GBS_FP_FMA: the same terms accumulated with fused multiply-adds (one
+ *   rounding per term, as the artifact's own nvcc build contracts them); the
+ *   term order may differ. Results agree with the CPU path within the parity
+ *   tolerance (normwise 1e-5 float, 1e-12 double). */
+enum { GBS_FP_EXACT = 0, GBS_FP_FMA = 1 };
+
+typedef struct gbs_desc {
+  int stencil;       /* gbs_stencil_id("star2d1r"), ... */
+  int dtype;         /* GBS_F32 | GBS_F64: the reference's SB_TYPE */
+  int n[3];          /* interior extent per axis (the reference's compsize on
+                        every axis); n[2] is ignored for 2-D stencils */
+  int timestep;      /* T >= 0 */
+  int fp_mode;       /* GBS_FP_EXACT | GBS_FP_FMA */
+  int bt;            /* timesteps fused per launch (temporal degree); 0 = tuned */
+  int bs1;           /* 2-D: warps per CTA; 3-D: tile rows (warps) per CTA; 0 = tuned */
+  int bs2;           /* reserved for the 3-D tile width; 0 */
+  int sl;            /* stream block length in rows (2-D) / planes (3-D); 0 = tuned */
+  const void *coef;  /* NULL: the source literals. Else nterms values of dtype,
+                        term order as in the source (the gradient form takes
+                        its numerator in coef[0]) */
+  double divisor;    /* stencils with a divisor (j2d5pt: /118): 0 = source value */
+  double eps;        /* gradient2d's epsilon: 0 = source value (0.0001f) */
+} gbs_desc;
+
+/* Device-side layout of a two-plane grid. Rows (the innermost axis) are
+ * padded to `pitch` elements and column c of a row is stored at element
+ * `shift + c`, so that every 16-byte-aligned window a kernel streams is
+ * inside the allocation. */
+typedef struct gbs_layout {
+  size_t pitch;      /* elements between consecutive rows */
+  size_t shift;      /* element offset of column 0 within a row */
+  size_t rows;       /* rows per plane: d0 (2-D) or d0*d1 (3-D) */
+  size_t plane;      /* elements per time plane (rows * pitch) */
+  size_t bytes;      /* bytes of the two-plane device buffer */
+  int dimsize[3];    /* n + 2r per axis (1 for unused axes) */
+  int dim, rad;
+} gbs_layout;
+
+/* The launch sequence the engine will run for a descriptor. */
+typedef struct gbs_plan_info {
+  int bt;            /* temporal degree chosen */
+  int bs1, bs2, sl;  /* tile / stream parameters chosen */
+  int launches;      /* kernel launches for the whole time loop */
+  int ctas;          /* CTAs per full-degree launch */
+  int valid_w;       /* valid (non-overlap) output columns per warp strip */
+  double redundancy; /* computed cells / useful cells per launch */
+} gbs_plan_info;
+
+/* ---- stencil catalogue ------------------------------------------------ */
+int gbs_num_stencils(void);
+const char *gbs_stencil_name(int id);
+int gbs_stencil_id(const char *name); /* -1 if unknown */
+/* dim, radius, terms in the update expression, BENCH_FPP (<stencil>.c:1-3) */
+gbs_status gbs_stencil_info(int id, int *dim, int *rad, int *nterms, int *fpp);
+
+/* ---- drop-in time loop ------------------------------------------------ */
+/* Replaces kernel_stencil(A1, compsize, timestep, scop=true)
+ * (common.h:42; generated host sequencer compiled/float/
+ * star2d1r-256-10-256_host.cu:10-566). host_A is the dense two-plane grid;
+ * both planes are copied to the device, advanced d->timestep steps and copied
+ * back. *ms_out (may be NULL) receives the device time of the time loop only,
+ * excluding allocation and copies, as the reference's return value does
+ * (_host.cu:39-40,559-560). The device buffer is cached between calls. */
+gbs_status gbs_run(const gbs_desc *d, void *host_A, double *ms_out);
+
+/* Same time loop on a device buffer in the engine's layout (gbs_get_layout),
+ * enqueued on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * Asynchronous: completion and device-side errors are reported by the next
+ * gbs_sync(stream). */
+gbs_status gbs_run_device(const gbs_desc *d, void *dev_A, void *stream);
+
+gbs_status gbs_get_layout(const gbs_desc *d, gbs_layout *out);
+gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out);
+
+/* Dense host grid <-> engine layout, both planes, enqueued on `stream`. */
+gbs_status gbs_upload(const gbs_desc *d, const void *host_A, void *dev_A, void *stream);
+gbs_status gbs_download(const gbs_desc *d, const void *dev_A, void *host_A, void *stream);
+
+/* Waits for `stream` and turns a device-side error word (a bounded wait that
+ * gave up) into GBS_ERR_TIMEOUT. */
+gbs_status gbs_sync(void *stream);
+
+const char *gbs_last_error(void);
+/* Frees the cached device buffers of gbs_run. */
+void gbs_release_cache(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBSTENCIL_H */
