@@ -70,10 +70,7 @@ static const Picks &picks(int sid, int dtype, int fma) {
   return table[sid][dtype][fma];
 }
 
-int max_bt(int sid, int dtype, int fma) {
-  const Picks &p = picks(sid, dtype, fma);
-  return p.ncls ? p.cls[p.ncls - 1] : 0;
-}
+int max_bt(int sid, int dtype, int fma) { return picks(sid, dtype, fma).maxb; }
 
 // ---------------------------------------------------------------------------
 // descriptors and layout
@@ -153,25 +150,50 @@ std::vector<int> split_steps(int T, int bt) {
   return out;
 }
 
-Geometry2D geometry2d(const Layout &L, int b, int sl_req, int sid) {
+static int sm_count() {
+  static int n = -1;
+  if (n < 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+      n = v;
+    else
+      n = 152;  // GB300
+  }
+  return n;
+}
+
+long long resident_warps_2d(int sid, int dtype, int fma, int b) {
+  static std::mutex mu;
+  static int cache[kNumStencils][2][2][kMaxB + 1];
+  std::lock_guard<std::mutex> lk(mu);
+  int &c = cache[sid][dtype][fma][b];
+  if (c == 0) {
+    const Picks &pk = picks(sid, dtype, fma);
+    int w = (b <= kMaxB && pk.o2[b]) ? pk.o2[b]() : 0;
+    c = w > 0 ? w : 16;
+  }
+  return (long long)c * sm_count();
+}
+
+Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident) {
   Geometry2D g{};
   const int R = L.rad, V = L.V;
   g.b = b;
   g.wout = ((32 * V - 2 * b * R - (V - 1)) / V) * V;
   const int ni = L.dims[0] - 2 * R, nj = L.dims[1] - 2 * R;
-  g.nstrips = (nj + g.wout - 1) / g.wout;
+  g.nstrips = g.wout > 0 ? (nj + g.wout - 1) / g.wout : 1;
   int sl = sl_req;
   if (sl <= 0) {
-    // about two waves of 16 warps per SM over 152 SMs, but blocks at least
-    // 8*b*r rows long so that the stream overlap stays small
-    const long long target = 152LL * 16 * 2;
-    long long nb = std::max<long long>(1, target / std::max(1, g.nstrips));
+    // one full wave of resident warps, each streaming one block; blocks at
+    // least 4*b*r rows long so that the stream overlap stays small
+    if (resident <= 0) resident = 152LL * 16;
+    long long nb = std::max<long long>(1, resident / std::max(1, g.nstrips));
     sl = (int)((ni + nb - 1) / nb);
-    sl = std::max(sl, std::max(16, 8 * b * R));
+    sl = std::max(sl, std::max(8, 4 * b * R));
   }
   g.sl = std::min(sl, ni);
   g.nblocks = (ni + g.sl - 1) / g.sl;
-  (void)sid;
   return g;
 }
 
@@ -245,13 +267,13 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
   const gbs_stencil_def_t *s = stencil_def(d->stencil);
   const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
   const Picks &pk = picks(d->stencil, d->dtype, fma);
-  if (pk.ncls == 0)
+  if (pk.maxb == 0)
     return fail(GBS_ERR_UNSUPPORTED, "no kernels built for %s dtype=%d fp_mode=%d", s->name, d->dtype,
                 d->fp_mode);
   int bt = d->bt > 0 ? d->bt : default_bt(d);
-  if (bt > pk.cls[pk.ncls - 1])
+  if (bt > pk.maxb)
     return fail(GBS_ERR_UNSUPPORTED, "bt=%d exceeds the largest fused degree built for %s (%d)", bt,
-                s->name, pk.cls[pk.ncls - 1]);
+                s->name, pk.maxb);
   // coefficients
   std::vector<double> coef(s->nterms > 0 ? s->nterms : 1);
   if (s->kind == 1) {
@@ -271,12 +293,10 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
   const size_t plane_bytes = (size_t)L.plane * L.esize;
   for (size_t j = 0; j < steps.size(); ++j) {
     const int b = steps[j];
-    int c = 0;
-    while (pk.cls[c] < b) ++c;
     const void *src = base + (j % 2) * plane_bytes;
     void *dst = base + ((j + 1) % 2) * plane_bytes;
     if (s->dim == 2) {
-      Geometry2D g = geometry2d(L, b, d->sl, d->stencil);
+      Geometry2D g = geometry2d(L, b, d->sl, resident_warps_2d(d->stencil, d->dtype, fma, b));
       gbs_status st = validate2d(L, g);
       if (st != GBS_OK) return st;
       Launch2D a{};
@@ -295,7 +315,8 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
       a.coef = coef.data();
       a.div = div;
       a.eps = eps;
-      cudaError_t e = pk.l2[c](a, stream);
+      if (!pk.l2[b]) return fail(GBS_ERR_UNSUPPORTED, "no 2-D kernel for b=%d", b);
+      cudaError_t e = pk.l2[b](a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");
     } else {
       return fail(GBS_ERR_UNSUPPORTED, "3-D stencils are not built in this configuration");
@@ -367,7 +388,7 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
   out->bt = bt;
   out->launches = (int)split_steps(d->timestep, bt).size();
   if (s->dim == 2) {
-    Geometry2D g = geometry2d(L, bt, d->sl, d->stencil);
+    Geometry2D g = geometry2d(L, bt, d->sl, resident_warps_2d(d->stencil, d->dtype, fma, bt));
     st = validate2d(L, g);
     if (st != GBS_OK) return st;
     out->bs1 = 4;

@@ -33,7 +33,9 @@ const gbs_stencil_def_t *stencil_def(int sid);
 gbs_status check_desc(const gbs_desc *d);
 Layout make_layout(const gbs_desc *d);
 std::vector<int> split_steps(int T, int bt);
-Geometry2D geometry2d(const Layout &L, int b, int sl_req, int sid);
+// resident_warps: warps the GPU holds at once for this kernel (0 = unknown)
+Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident_warps);
+long long resident_warps_2d(int sid, int dtype, int fma, int b);
 gbs_status validate2d(const Layout &L, const Geometry2D &g);
 gbs_status error_word(int **out);
 gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_t stream, int *err);

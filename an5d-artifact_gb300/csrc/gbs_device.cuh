@@ -201,29 +201,89 @@ __device__ __forceinline__ T term_next(T acc, T c, T a) {
   else return A::add(acc, A::mul(c, a));
 }
 
-// gradient2d.c:17-21: u + num / sqrt(eps + sum_n (u - u_n)^2). In exact mode
-// the squares are summed in T and, as C evaluates `1.0f / sqrt(x)`, the root,
-// the quotient and the final sum are taken in double before rounding to T.
-// In FMA mode the squares are fused and a T-precision IEEE root and quotient
-// are used.
-template <typename T, bool FMA, int NN>
+// gradient2d.c:17-21: u + num / sqrt(eps + sum_n (u - u_n)^2), evaluated as
+// C evaluates it: the differences and squares summed in T, each rounded, then
+// (since `1.0f / sqrt(x)` calls the double sqrt) the root, the quotient and
+// the final sum in double, rounded once to T. Both fp modes use this form:
+// the update amplifies rounding where neighbours agree, so even fusing the
+// squares drifts past the 1e-5 parity bound within ten steps, and the double
+// root and quotient dominate its cost either way.
+template <typename T, int NN>
 __device__ __forceinline__ T gradient_update(T u, const T (&nb)[NN], T eps, T num) {
   using A = Arith<T>;
   T s = eps;
 #pragma unroll
   for (int n = 0; n < NN; ++n) {
     const T d = A::sub(u, nb[n]);
-    if constexpr (FMA) s = A::fma(d, d, s);
-    else s = A::add(s, A::mul(d, d));
+    s = A::add(s, A::mul(d, d));
   }
-  if constexpr (!FMA || std::is_same<T, double>::value) {
-    const double q = __ddiv_rn((double)num, __dsqrt_rn((double)s));
-    const double r = __dadd_rn((double)u, q);
-    if constexpr (std::is_same<T, float>::value) return __double2float_rn(r);
-    else return r;
-  } else {
-    return A::add(u, A::div(num, __fsqrt_rn(s)));
+  const double q = __ddiv_rn((double)num, __dsqrt_rn((double)s));
+  const double r = __dadd_rn((double)u, q);
+  if constexpr (std::is_same<T, float>::value) return __double2float_rn(r);
+  else return r;
+}
+
+// x / d, correctly rounded, for a divisor d known in advance with y =
+// RN(1/d) (y == 0 marks a divisor outside [2^-16, 2^16] (float) or
+// [2^-50, 2^50] (double): IEEE division only). A reciprocal product with one
+// FMA correction (Markstein's scheme) gives q1; q1 is returned only when the
+// exact remainder r1 = x - q1*d shows that x/d lies strictly between the two
+// rounding midpoints around q1, which makes q1 = RN(x/d). In the guarded
+// range r1 is exact (the remainder of a faithful quotient is representable)
+// and so are the midpoint bounds |d|*ulp/2 (power-of-two scalings); outside
+// it, or when the test fails (x/d within an ulp fraction of a midpoint), the
+// IEEE division is used. gbs_check_division compares this with IEEE division.
+__device__ __forceinline__ float div_by(float x, float d, float y) {
+  if (y != 0.0f) {
+    const float q0 = __fmul_rn(x, y);
+    const float r = __fmaf_rn(-q0, d, x);
+    const float q1 = __fmaf_rn(r, y, q0);
+    const float a = fabsf(q1);
+    if (a >= 0x1p-80f && a <= 0x1p+100f) {
+      const float r1 = __fmaf_rn(-q1, d, x);
+      const int ab = __float_as_int(a);
+      const float u = __int_as_float((ab & 0x7f800000) - (23 << 23));  // ulp(q1)
+      const bool pow2 = (ab & 0x007fffff) == 0;
+      // offset of x/d from q1, times |d|, signed positive away from zero
+      const float om = ((d < 0.0f) != (q1 < 0.0f)) ? -r1 : r1;
+      const float ad = fabsf(d);
+      const float lim = (om >= 0.0f || !pow2) ? __fmul_rn(ad, __fmul_rn(u, 0.5f))
+                                              : __fmul_rn(ad, __fmul_rn(u, 0.25f));
+      if (fabsf(om) < lim) return q1;
+    }
   }
+  if (x == 0.0f && y != 0.0f) return __fmul_rn(x, y);
+  return __fdiv_rn(x, d);
+}
+__device__ __forceinline__ double div_by(double x, double d, double y) {
+  if (y != 0.0) {
+    const double q0 = __dmul_rn(x, y);
+    const double r = __fma_rn(-q0, d, x);
+    const double q1 = __fma_rn(r, y, q0);
+    const double a = fabs(q1);
+    if (a >= 0x1p-900 && a <= 0x1p+900) {
+      const double r1 = __fma_rn(-q1, d, x);
+      const long long ab = __double_as_longlong(a);
+      const double u = __longlong_as_double((ab & 0x7ff0000000000000ll) - (52ll << 52));
+      const bool pow2 = (ab & 0x000fffffffffffffll) == 0;
+      const double om = ((d < 0.0) != (q1 < 0.0)) ? -r1 : r1;
+      const double ad = fabs(d);
+      const double lim = (om >= 0.0 || !pow2) ? __dmul_rn(ad, __dmul_rn(u, 0.5))
+                                              : __dmul_rn(ad, __dmul_rn(u, 0.25));
+      if (fabs(om) < lim) return q1;
+    }
+  }
+  if (x == 0.0 && y != 0.0) return __dmul_rn(x, y);
+  return __ddiv_rn(x, d);
+}
+
+// RN(1/d) for div_by, or 0 when d is outside the range div_by's test covers.
+template <typename T> inline T div_reciprocal(double d) {
+  const double lo = sizeof(T) == 4 ? 0x1p-16 : 0x1p-50, hi = sizeof(T) == 4 ? 0x1p+16 : 0x1p+50;
+  const double ad = d < 0 ? -d : d;
+  if (!(ad >= lo && ad <= hi)) return (T)0;
+  volatile T one = (T)1;
+  return one / (T)d;
 }
 
 }  // namespace gbs

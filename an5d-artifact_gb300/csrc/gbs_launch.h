@@ -33,16 +33,18 @@ struct Launch3D {
 };
 
 using Launch2DFn = cudaError_t (*)(const Launch2D &, cudaStream_t);
+// resident warps per SM of a 2-D launcher (occupancy), 0 on error
+using Occupancy2DFn = int (*)();
 using Launch3DFn = cudaError_t (*)(const Launch3D &, cudaStream_t);
 
-// Launchers of one (stencil, element type, fp mode): one per fused-degree
-// class; class c handles any b <= cls[c].
+// Launchers of one (stencil, element type, fp mode), indexed by the fused
+// degree b (nullptr where none is built).
+constexpr int kMaxB = 16;
 struct Picks {
-  int ncls;
-  int cls[4];
-  Launch2DFn l2[4];
-  Launch3DFn l3[4];
-  int smem3[4];       // dynamic shared memory of the 3-D launchers (bytes)
+  int maxb;
+  Launch2DFn l2[kMaxB + 1];
+  Occupancy2DFn o2[kMaxB + 1];
+  Launch3DFn l3[kMaxB + 1];
 };
 
 }  // namespace gbs

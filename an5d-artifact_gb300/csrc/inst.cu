@@ -18,33 +18,34 @@ constexpr bool kFma = GBS_FMA != 0;
 // Fused-degree classes worth instantiating. A b-level strip loses 2*b*r of
 // its 32*V columns to overlap, and stencils with many terms are FP-bound
 // before temporal blocking pays; FP64 on GB300 is FP-bound already at b=1.
+// Exact mode spends two FP instructions per term, so its best degree is
+// lower; it keeps degrees up to 4.
 constexpr int max_class() {
   if (S::kDim == 2) {
     if (sizeof(T) == 8) return 2;
-    if (S::kKind == KIND_GRADIENT) return kFma ? 8 : 2;
-    if (S::kAssoc) return S::kRad == 1 ? 8 : (S::kRad == 2 ? 4 : 2);
-    return S::kRad <= 2 ? 8 : 4;
+    if (S::kKind == KIND_GRADIENT) return 2;  // FP64 root and quotient
+    const int cap = kFma ? 8 : 4;
+    if (S::kAssoc) return S::kRad == 1 ? cap : (S::kRad == 2 ? 4 : 2);
+    return S::kRad <= 2 ? cap : 4;
   }
   return 1;
 }
 
-template <int B> void add2(Picks &p) {
-  if constexpr (S::kDim == 2 && B <= max_class()) {
-    p.cls[p.ncls] = B;
-    p.l2[p.ncls] = &launch2d<S, T, B, kFma>;
-    p.l3[p.ncls] = nullptr;
-    p.smem3[p.ncls] = 0;
-    ++p.ncls;
+template <int B> void add(Picks &p) {
+  if constexpr (B <= max_class()) {
+    if constexpr (S::kDim == 2) {
+      p.l2[B] = &launch2d<S, T, B, kFma>;
+      p.o2[B] = &occupancy2d<S, T, B, kFma>;
+    }
+    p.maxb = B;
   }
 }
+template <int... Bs> void add_all(Picks &p, std::integer_sequence<int, Bs...>) { (add<Bs + 1>(p), ...); }
 }  // namespace
 
 Picks GBS_PICK() {
   Picks p{};
-  add2<1>(p);
-  add2<2>(p);
-  add2<4>(p);
-  add2<8>(p);
+  add_all(p, std::make_integer_sequence<int, kMaxB>());
   return p;
 }
 }  // namespace gbs

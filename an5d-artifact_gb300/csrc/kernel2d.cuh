@@ -48,11 +48,11 @@ template <typename T, int NT> struct Params2D {
   long long pitch;     // elements per padded row
   int d0, d1;          // dimsize: rows, columns (interior + 2r)
   int shift;           // column c is stored at element shift + c
-  int b;               // time levels fused in this launch (1..BTMAX)
+  int b;               // time levels fused in this launch (the kernel's B)
   int wout;            // output columns per strip (multiple of V)
   int nstrips, nblocks, sl;
   T coef[NT];
-  T div, eps;
+  T div, rdiv, eps;    // divisor, RN(1/divisor), gradient epsilon
 };
 
 // Compile-time facts about a stencil's term list.
@@ -95,7 +95,123 @@ __device__ __forceinline__ void extend_row(T (&ext)[V + 2 * ST::kRad], const T (
 template <bool UNR, int W>
 __host__ __device__ constexpr int wslot(int ph, int j) { return UNR ? (ph + 1 + j) % W : j; }
 
-template <class ST, typename T, int BTMAX, bool FMA, int WPC, int NSTAGE>
+// One fused time level: the level-(l) row x arrives, the level-(l+1) row q
+// leaves in x. CAREFUL handles halo rows and columns (grid edges);
+// otherwise the caller guarantees that every row and column is interior.
+template <class ST, typename T, bool FMA, bool UNR, bool CAREFUL, int PH, int V>
+__device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V], int q, bool edge,
+                                        int col0, const T *src_row_base,
+                                        const Params2D<T, ST::kTerms> &p) {
+  constexpr int R = ST::kRad;
+  constexpr int W = 2 * R + 1;
+  using A = Arith<T>;
+  T y[V];
+  bool halo_row = false;
+  if constexpr (CAREFUL) halo_row = (q < R) || (q >= p.d0 - R);
+  if constexpr (!ST::kAssoc) {
+#pragma unroll
+    for (int e = 0; e < V; ++e) win[wslot<UNR, W>(PH, 2 * R)][e] = x[e];
+    constexpr int cslot = wslot<UNR, W>(PH, R);
+    if (CAREFUL && halo_row) {
+#pragma unroll
+      for (int e = 0; e < V; ++e) y[e] = win[cslot][e];
+    } else {
+      if constexpr (ST::kKind == KIND_GRADIENT) {
+        T ext[V + 2 * R];
+        extend_row<ST, V, 0>(ext, win[cslot]);
+        static_for<V>([&](auto EI) {
+          constexpr int e = decltype(EI)::value;
+          T nb[ST::kTerms];
+          static_for<ST::kTerms>([&](auto TI) {
+            constexpr int t = decltype(TI)::value;
+            constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+            if constexpr (di == 0) nb[t] = ext[R + e + dj];
+            else nb[t] = win[wslot<UNR, W>(PH, R + di)][e];
+          });
+          y[e] = gradient_update<T, ST::kTerms>(win[cslot][e], nb, p.eps, p.coef[0]);
+        });
+      } else {
+        T ext[W][V + 2 * R];
+        static_for<W>([&](auto DI) {
+          constexpr int di = decltype(DI)::value - R;
+          if constexpr (Tap2<ST, V>::row_has_dj(di))
+            extend_row<ST, V, di>(ext[di + R], win[wslot<UNR, W>(PH, R + di)]);
+        });
+        static_for<ST::kTerms>([&](auto TI) {
+          constexpr int t = decltype(TI)::value;
+          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+          constexpr int slot = wslot<UNR, W>(PH, R + di);
+#pragma unroll
+          for (int e = 0; e < V; ++e) {
+            const T a = (dj == 0) ? win[slot][e] : ext[di + R][R + e + dj];
+            if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
+            else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
+          }
+        });
+        if constexpr (ST::kHasDiv) {
+#pragma unroll
+          for (int e = 0; e < V; ++e) y[e] = div_by(y[e], p.div, p.rdiv);
+        }
+      }
+      if (CAREFUL && edge) {
+#pragma unroll
+        for (int e = 0; e < V; ++e)
+          if (col0 + e < R || col0 + e >= p.d1 - R) y[e] = win[cslot][e];
+      }
+    }
+  } else {
+    // assoc: the arriving row m = q + R adds its terms to outputs q..q+2R
+    T ext[V + 2 * R];
+    static_for<V + 2 * R>([&](auto XI) {
+      constexpr int xx = decltype(XI)::value - R;
+      constexpr bool any = [] {
+        for (int di = -R; di <= R; ++di)
+          if (Tap2<ST, V>::need(di, xx)) return true;
+        return false;
+      }();
+      if constexpr (any) ext[R + xx] = row_elem<V, xx>(x);
+    });
+    static_for<ST::kTerms>([&](auto TI) {
+      constexpr int t = decltype(TI)::value;
+      constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+      constexpr int slot = wslot<UNR, W>(PH, R - di);
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const T a = ext[R + e + dj];
+        if constexpr (t == 0) win[slot][e] = A::mul(p.coef[t], a);
+        else win[slot][e] = term_next<T, FMA>(win[slot][e], p.coef[t], a);
+      }
+    });
+    constexpr int oslot = wslot<UNR, W>(PH, 0);
+#pragma unroll
+    for (int e = 0; e < V; ++e) y[e] = win[oslot][e];
+    if constexpr (ST::kHasDiv) {
+#pragma unroll
+      for (int e = 0; e < V; ++e) y[e] = div_by(y[e], p.div, p.rdiv);
+    }
+    if constexpr (CAREFUL) {
+      if (halo_row) {
+        if (q >= 0 && q < p.d0) ld_vec_global<T, V>(y, src_row_base + (long long)q * p.pitch);
+      } else if (edge) {
+        T c[V];
+        ld_vec_global<T, V>(c, src_row_base + (long long)q * p.pitch);
+#pragma unroll
+        for (int e = 0; e < V; ++e)
+          if (col0 + e < R || col0 + e >= p.d1 - R) y[e] = c[e];
+      }
+    }
+  }
+  if constexpr (!UNR) {
+#pragma unroll
+    for (int j = 0; j < 2 * R; ++j)
+#pragma unroll
+      for (int e = 0; e < V; ++e) win[j][e] = win[j + 1][e];
+  }
+#pragma unroll
+  for (int e = 0; e < V; ++e) x[e] = y[e];
+}
+
+template <class ST, typename T, int B, bool FMA, int WPC, int NSTAGE>
 __global__ void __launch_bounds__(WPC * 32)
     stencil2d_kernel(const __grid_constant__ Params2D<T, ST::kTerms> p) {
   constexpr int V = 16 / sizeof(T);
@@ -105,7 +221,6 @@ __global__ void __launch_bounds__(WPC * 32)
   constexpr int NPH = UNR ? W : 1;
   constexpr int ROW = 32 * V;
   constexpr unsigned ROW_BYTES = ROW * sizeof(T);
-  using A = Arith<T>;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -114,28 +229,30 @@ __global__ void __launch_bounds__(WPC * 32)
   if (gw >= (long long)p.nstrips * p.nblocks) return;
   const int strip = (int)(gw % p.nstrips);
   const int blk = (int)(gw / p.nstrips);
-  const int b = p.b;
 
   // ---- columns (column space c; offset space c + shift) ----
   const int cs = R + strip * p.wout;
   const int ce = min(cs + p.wout, p.d1 - R);
-  const int need_lo = max(0, cs - b * R);
+  const int need_lo = max(0, cs - B * R);
   const int ws = ((need_lo + p.shift) / V) * V;
   const int col0 = ws - p.shift + lane * V;  // column of this lane's element 0
   const bool edge = (ws - p.shift < R) || (ws - p.shift + ROW > p.d1 - R);
+  const bool store_all = (col0 >= cs && col0 + V <= ce);
 
   // ---- rows ----
   const int i0 = R + blk * p.sl;
   const int i1 = min(i0 + p.sl, p.d0 - R);
-  const int pstart = max(0, i0 - b * R);
-  const int pend = min(p.d0, i1 + b * R);  // rows loaded: [pstart, pend)
-  const int plast = i1 - 1 + b * R;        // last pipeline step
+  const int pstart = max(0, i0 - B * R);
+  const int pend = min(p.d0, i1 + B * R);  // rows loaded: [pstart, pend)
+  const int plast = i1 - 1 + B * R;        // last pipeline step
   const int nload = pend - pstart;
 
   T *ring = reinterpret_cast<T *>(smem_raw) + (size_t)wid * NSTAGE * ROW;
   uint64_t *bars =
       reinterpret_cast<uint64_t *>(smem_raw + (size_t)WPC * NSTAGE * ROW_BYTES) + wid * NSTAGE;
   const T *src_win = p.src + ws;
+  const T *src_lane = src_win + lane * V;
+  T *dst_lane = p.dst + ws + lane * V;
 
   if (lane == 0) {
 #pragma unroll
@@ -150,9 +267,9 @@ __global__ void __launch_bounds__(WPC * 32)
   }
   __syncwarp();
 
-  T win[BTMAX][W][V];
+  T win[B][W][V];
 #pragma unroll
-  for (int l = 0; l < BTMAX; ++l)
+  for (int l = 0; l < B; ++l)
 #pragma unroll
     for (int w = 0; w < W; ++w)
 #pragma unroll
@@ -161,161 +278,74 @@ __global__ void __launch_bounds__(WPC * 32)
   int consumed = 0;  // loads consumed so far (for the drain on timeout)
   bool ok = true;
 
-#pragma unroll 1
-  for (int pb = pstart; pb <= plast && ok; pb += NPH) {
-    static_for<NPH>([&](auto PH) {
-      constexpr int ph = decltype(PH)::value;
-      const int pp = pb + ph;
-      if (!ok || pp > plast) return;
-
-      // ---- level 0: row pp from the ring ----
-      T x[V];
-      if (pp < pend) {
-        const int n = pp - pstart;
-        const int s = n % NSTAGE;
-        // every lane waits; the decision to give up is warp-uniform
-        const bool got = mbar_wait(&bars[s], (unsigned)(n / NSTAGE) & 1u, nullptr, 0);
-        if (!__all_sync(0xffffffffu, got)) {
-          if (lane == 0) atomicOr(p.err, ERR_WAIT_TIMEOUT);
-          ok = false;
-          return;
-        }
-        ld_vec<T, V>(x, ring + s * ROW + lane * V);
-        consumed = n + 1;
-        __syncwarp();
-        if (lane == 0 && n + NSTAGE < nload) {
-          mbar_arrive_expect_tx(&bars[s], ROW_BYTES);
-          bulk_g2s(ring + s * ROW, src_win + (long long)(pp + NSTAGE) * p.pitch, ROW_BYTES,
-                   &bars[s]);
-        }
+  // One pipeline step at row pp with phase PH. CAREFUL steps handle the
+  // stream ends, halo rows and edge columns; the others assume none occur.
+  auto step = [&](auto PHI, auto CAREI, int pp) {
+    constexpr int ph = decltype(PHI)::value;
+    constexpr bool careful = decltype(CAREI)::value;
+    T x[V];
+    if (!careful || pp < pend) {
+      const int n = pp - pstart;
+      const int s = n % NSTAGE;
+      // every lane waits; the decision to give up is warp-uniform
+      const bool got = mbar_wait(&bars[s], (unsigned)(n / NSTAGE) & 1u, nullptr, 0);
+      if (!__all_sync(0xffffffffu, got)) {
+        if (lane == 0) atomicOr(p.err, ERR_WAIT_TIMEOUT);
+        ok = false;
+        return;
+      }
+      ld_vec<T, V>(x, ring + s * ROW + lane * V);
+      consumed = n + 1;
+      __syncwarp();
+      if (lane == 0 && n + NSTAGE < nload) {
+        mbar_arrive_expect_tx(&bars[s], ROW_BYTES);
+        bulk_g2s(ring + s * ROW, src_win + (long long)(pp + NSTAGE) * p.pitch, ROW_BYTES, &bars[s]);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < V; ++e) x[e] = T(0);
+    }
+    static_for<B>([&](auto LI) {
+      constexpr int l = decltype(LI)::value;
+      level2d<ST, T, FMA, UNR, careful, ph, V>(win[l], x, pp - (l + 1) * R, edge, col0, src_lane, p);
+    });
+    const int q = pp - B * R;
+    if (q >= i0 && q < i1) {
+      T *d = dst_lane + (long long)q * p.pitch;
+      if (store_all) {
+        st_vec<T, V>(d, x);
       } else {
 #pragma unroll
-        for (int e = 0; e < V; ++e) x[e] = T(0);
+        for (int e = 0; e < V; ++e)
+          if (col0 + e >= cs && col0 + e < ce) d[e] = x[e];
       }
+    }
+  };
 
-      // ---- fused time levels ----
-      static_for<BTMAX>([&](auto LI) {
-        constexpr int l = decltype(LI)::value;
-        if (l >= b) return;
-        const int q = pp - (l + 1) * R;  // row produced by level l+1
-        const bool halo_row = (q < R) || (q >= p.d0 - R);
-        T y[V];
-        if constexpr (!ST::kAssoc) {
-          // direct: push the new row, evaluate the centre row q
-#pragma unroll
-          for (int e = 0; e < V; ++e) win[l][wslot<UNR, W>(ph, 2 * R)][e] = x[e];
-          constexpr int cslot = wslot<UNR, W>(ph, R);
-          if (halo_row) {
-#pragma unroll
-            for (int e = 0; e < V; ++e) y[e] = win[l][cslot][e];
-          } else {
-            if constexpr (ST::kKind == KIND_GRADIENT) {
-              T ext[V + 2 * R];
-              extend_row<ST, V, 0>(ext, win[l][cslot]);
-              static_for<V>([&](auto EI) {
-                constexpr int e = decltype(EI)::value;
-                T nb[ST::kTerms];
-                static_for<ST::kTerms>([&](auto TI) {
-                  constexpr int t = decltype(TI)::value;
-                  constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-                  if constexpr (di == 0) nb[t] = ext[R + e + dj];
-                  else nb[t] = win[l][wslot<UNR, W>(ph, R + di)][e];
-                });
-                y[e] = gradient_update<T, FMA, ST::kTerms>(win[l][cslot][e], nb, p.eps, p.coef[0]);
-              });
-            } else {
-              // rows with off-centre columns get their lane-extended copy once
-              T ext[W][V + 2 * R];
-              static_for<W>([&](auto DI) {
-                constexpr int di = decltype(DI)::value - R;
-                if constexpr (Tap2<ST, V>::row_has_dj(di))
-                  extend_row<ST, V, di>(ext[di + R], win[l][wslot<UNR, W>(ph, R + di)]);
-              });
-              static_for<ST::kTerms>([&](auto TI) {
-                constexpr int t = decltype(TI)::value;
-                constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-                constexpr int slot = wslot<UNR, W>(ph, R + di);
-#pragma unroll
-                for (int e = 0; e < V; ++e) {
-                  const T a = (dj == 0) ? win[l][slot][e] : ext[di + R][R + e + dj];
-                  if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
-                  else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
-                }
-              });
-              if constexpr (ST::kHasDiv) {
-#pragma unroll
-                for (int e = 0; e < V; ++e) y[e] = A::div(y[e], p.div);
-              }
-            }
-            if (edge) {
-#pragma unroll
-              for (int e = 0; e < V; ++e)
-                if (col0 + e < R || col0 + e >= p.d1 - R) y[e] = win[l][cslot][e];
-            }
-          }
-        } else {
-          // assoc: the arriving row m = q + R adds its terms to outputs q..q+2R
-          T ext[V + 2 * R];
-          static_for<V + 2 * R>([&](auto XI) {
-            constexpr int xx = decltype(XI)::value - R;
-            bool any = false;
-            static_for<W>([&](auto DI) {
-              constexpr int di = decltype(DI)::value - R;
-              if constexpr (Tap2<ST, V>::need(di, xx)) any = true;
-            });
-            if (any) ext[R + xx] = row_elem<V, xx>(x);
-          });
-          static_for<ST::kTerms>([&](auto TI) {
-            constexpr int t = decltype(TI)::value;
-            constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-            constexpr int slot = wslot<UNR, W>(ph, R - di);
-#pragma unroll
-            for (int e = 0; e < V; ++e) {
-              const T a = ext[R + e + dj];
-              if constexpr (t == 0) win[l][slot][e] = A::mul(p.coef[t], a);
-              else win[l][slot][e] = term_next<T, FMA>(win[l][slot][e], p.coef[t], a);
-            }
-          });
-          constexpr int oslot = wslot<UNR, W>(ph, 0);
-#pragma unroll
-          for (int e = 0; e < V; ++e) y[e] = win[l][oslot][e];
-          if constexpr (ST::kHasDiv) {
-#pragma unroll
-            for (int e = 0; e < V; ++e) y[e] = A::div(y[e], p.div);
-          }
-          if (halo_row) {
-            if (q >= 0 && q < p.d0) ld_vec_global<T, V>(y, p.src + (long long)q * p.pitch + ws + lane * V);
-          } else if (edge) {
-            T c[V];
-            ld_vec_global<T, V>(c, p.src + (long long)q * p.pitch + ws + lane * V);
-#pragma unroll
-            for (int e = 0; e < V; ++e)
-              if (col0 + e < R || col0 + e >= p.d1 - R) y[e] = c[e];
-          }
-        }
-        if constexpr (!UNR) {
-#pragma unroll
-          for (int j = 0; j < 2 * R; ++j)
-#pragma unroll
-            for (int e = 0; e < V; ++e) win[l][j][e] = win[l][j + 1][e];
-        }
-#pragma unroll
-        for (int e = 0; e < V; ++e) x[e] = y[e];
+  // steps [lo, hi) in whole groups of NPH phases, starting at a group boundary
+  auto run = [&](int lo, int hi, auto CAREI) {
+#pragma unroll 1
+    for (int pb = lo; pb < hi && ok; pb += NPH) {
+      static_for<NPH>([&](auto PHI) {
+        const int pp = pb + decltype(PHI)::value;
+        if (!ok || (decltype(CAREI)::value && pp >= hi)) return;
+        step(PHI, CAREI, pp);
       });
-
-      // ---- store level b's row ----
-      const int q = pp - b * R;
-      if (q >= i0 && q < i1) {
-        T *d = p.dst + (long long)q * p.pitch + ws + lane * V;
-        if (col0 >= cs && col0 + V <= ce) {
-          st_vec<T, V>(d, x);
-        } else {
-#pragma unroll
-          for (int e = 0; e < V; ++e)
-            if (col0 + e >= cs && col0 + e < ce) d[e] = x[e];
-        }
-      }
-    });
+    }
+  };
+  const int steps = plast + 1 - pstart;
+  if (edge) {
+    run(pstart, plast + 1, IC<1>());
+  } else {
+    // rows whose levels all lie in the interior and that are loaded
+    const int mid_lo = max(pstart, (B + 1) * R);
+    const int mid_hi = min(plast + 1, p.d0);
+    int a = pstart + (mid_lo - pstart + NPH - 1) / NPH * NPH;
+    int z = pstart + max(0, mid_hi - pstart) / NPH * NPH;
+    if (a > z) a = z = pstart + steps;  // no interior stretch: all careful
+    run(pstart, min(a, plast + 1), IC<1>());
+    if (a < z) run(a, z, IC<0>());
+    if (z < plast + 1) run(z, plast + 1, IC<1>());
   }
 
   if (!ok && lane == 0) {
@@ -327,9 +357,22 @@ __global__ void __launch_bounds__(WPC * 32)
   }
 }
 
-template <class ST, typename T, int BTMAX, bool FMA>
+constexpr int kWpc2D = 4, kStages2D = 8;
+
+template <class ST, typename T, int B, bool FMA>
+int occupancy2d() {
+  constexpr int V = 16 / sizeof(T);
+  const size_t smem = (size_t)kWpc2D * kStages2D * (32 * V * sizeof(T) + sizeof(uint64_t));
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stencil2d_kernel<ST, T, B, FMA, kWpc2D, kStages2D>,
+                                                    kWpc2D * 32, smem) != cudaSuccess)
+    return 0;
+  return nb * kWpc2D;
+}
+
+template <class ST, typename T, int B, bool FMA>
 cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
-  constexpr int WPC = 4, NSTAGE = 8;
+  constexpr int WPC = kWpc2D, NSTAGE = kStages2D;
   constexpr int V = 16 / sizeof(T);
   Params2D<T, ST::kTerms> p;
   p.src = static_cast<const T *>(a.src);
@@ -346,11 +389,12 @@ cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
   p.sl = a.sl;
   for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = (T)a.coef[t];
   p.div = (T)a.div;
+  p.rdiv = div_reciprocal<T>(a.div);
   p.eps = (T)a.eps;
   const size_t smem = (size_t)WPC * NSTAGE * (32 * V * sizeof(T) + sizeof(uint64_t));
   const long long warps = (long long)a.nstrips * a.nblocks;
   const long long grid = (warps + WPC - 1) / WPC;
-  stencil2d_kernel<ST, T, BTMAX, FMA, WPC, NSTAGE><<<(unsigned)grid, WPC * 32, smem, stream>>>(p);
+  stencil2d_kernel<ST, T, B, FMA, WPC, NSTAGE><<<(unsigned)grid, WPC * 32, smem, stream>>>(p);
   return cudaGetLastError();
 }
 

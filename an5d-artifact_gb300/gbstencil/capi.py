@@ -66,6 +66,9 @@ SIGNATURES = [
     ("gbs_upload", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_download", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_sync", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("gbs_check_division", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_longlong,
+                                          ctypes.POINTER(ctypes.c_longlong)]),
     ("gbs_last_error", ctypes.c_char_p, []),
     ("gbs_release_cache", None, []),
 ]
@@ -167,6 +170,23 @@ def download(desc: Desc, dev_ptr: int, host_ptr: int, stream: int = 0):
 
 def sync(stream: int = 0):
     check(lib().gbs_sync(ctypes.c_void_p(stream)))
+
+
+def measure_fp_peak(dtype) -> float:
+    """Measured FMA throughput of the current device, GFLOP/s."""
+    g = ctypes.c_double(0.0)
+    dt = GBS_F32 if np.dtype(dtype) == np.float32 else GBS_F64
+    check(lib().gbs_measure_fp_peak(dt, ctypes.byref(g)))
+    return g.value
+
+
+def check_division(dtype, divisor: float, samples: int = 0) -> int:
+    """Inputs on which the engine's constant-divisor division differs from
+    IEEE division (see gbs_check_division)."""
+    m = ctypes.c_longlong(-1)
+    dt = GBS_F32 if np.dtype(dtype) == np.float32 else GBS_F64
+    check(lib().gbs_check_division(dt, float(divisor), int(samples), ctypes.byref(m)))
+    return m.value
 
 
 def kernel_stencil(A1: np.ndarray, compsize: int, timestep: int, scop: bool = True, *,

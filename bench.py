@@ -1,0 +1,333 @@
+"""Benchmark of the stencil time loop on GB300 (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload suite3d|star2d1r] [--fp-mode fma|exact]
+
+A step is one full time loop (T timesteps) over each grid of the workload:
+
+* suite3d (default): star3d2r and box3d1r, fp32 and fp64, 512^3 interior,
+  T=1000, each at the fused degree the planner picks.
+* star2d1r: star2d1r fp32, 4096^2 interior, T=100.
+
+Inputs are synthetic: every cell (halo included) i.i.d. U[0,1) from a fixed
+seed, coefficients U[0,1) normalised to sum 1. ``value`` is GCells/s
+(interior cell updates per second) with the grids resident in HBM; ``e2e`` is
+the same metric through the C ABI's host-buffer entry point gbs_run (pinned
+host grids copied in and out inside the timed region). The L2 is flushed
+(a 512 MB write) between timed steps.
+
+``--impl reference`` times the artifact's CPU path (the OpenMP restatement
+in oracle/, which is bit-identical to it) on the host cores, on a bounded
+sample of each grid (fewer timesteps), and reports the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT, ROOT / "oracle", ROOT / "an5d-artifact_gb300"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+import numpy as np  # noqa: E402
+
+METRIC = "GCells/s per stencil fp32/fp64 & % roofline; batched and adjoint vs plain"
+
+WORKLOADS = {
+    "suite3d": [("star3d2r", np.float32, 512, 1000), ("star3d2r", np.float64, 512, 1000),
+                ("box3d1r", np.float32, 512, 1000), ("box3d1r", np.float64, 512, 1000)],
+    "star2d1r": [("star2d1r", np.float32, 4096, 100)],
+}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def random_coefficients(name, dtype, seed):
+    from gbstencil import capi
+    s = capi.info(name)
+    rng = np.random.default_rng(seed)
+    c = rng.random(s["nterms"])
+    c = c / c.sum()
+    if s["divisor"]:
+        c = c * s["divisor"]
+    return c.astype(dtype)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for n, v in zip(names, s[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+# our engine
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import torch
+    from gbstencil import capi
+    from gbstencil.grid import DeviceGrid
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    work = WORKLOADS[args.workload]
+    grids, coefs, plans = [], [], []
+    for i, (name, dt, n, T) in enumerate(work):
+        g = DeviceGrid(name, dt, n, device=dev)
+        g.fill_uniform(seed=20250101 + i)
+        c = random_coefficients(name, dt, 1000 + i)
+        d, keep = g.desc(T, args.fp_mode, 0, 0, coef=c)
+        plans.append(capi.plan(d))
+        grids.append(g)
+        coefs.append(c)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    cells = sum(int(np.prod(g.n)) * T for g, (_, _, _, T) in zip(grids, work))
+
+    def step():
+        for g, c, (_, _, _, T) in zip(grids, coefs, work):
+            g.run(T, args.fp_mode, 0, 0, coef=c)
+
+    for _ in range(args.warmup):
+        step()
+    capi.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+
+    # device-resident timing, per grid (for the per-stencil breakdown)
+    per_grid_ms = [0.0] * len(grids)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in grids]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            for gi, (g, c, (_, _, _, T)) in enumerate(zip(grids, coefs, work)):
+                ev[gi][0].record(stream)
+                g.run(T, args.fp_mode, 0, 0, coef=c)
+                ev[gi][1].record(stream)
+            torch.cuda.synchronize()
+            for gi in range(len(grids)):
+                per_grid_ms[gi] += ev[gi][0].elapsed_time(ev[gi][1])
+    capi.sync(stream.cuda_stream)
+    total_ms = sum(per_grid_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = cells * world / (ms_per_step * 1e-3) / 1e9
+
+    # end to end through gbs_run with pinned host grids
+    e2e_ms, h2d, d2h = 0.0, 0, 0
+    hosts = []
+    for g in grids:
+        h = torch.empty((2,) + tuple(g.dimsize), dtype=g.buf.dtype).pin_memory()
+        h.copy_(torch.from_numpy(g.download()))
+        hosts.append(h)
+    def e2e_step():
+        nonlocal h2d, d2h
+        for g, h, c, (_, _, _, T) in zip(grids, hosts, coefs, work):
+            d, keep = capi.make_desc(g.name, g.dtype, g.n, T, args.fp_mode, coef=c)
+            capi.run_host(d, h.numpy())
+    e2e_step()  # allocates gbs_run's device buffer once
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps)
+    h2d = sum(int(h.numel()) * h.element_size() for h in hosts)
+    d2h = h2d
+
+    # roofline of the dominant grid (largest device time)
+    hbm, peak_kind = load_peaks()
+    gi = int(np.argmax(per_grid_ms))
+    name, dt, n, T = work[gi]
+    p = plans[gi]
+    S = np.dtype(dt).itemsize
+    ncell = int(np.prod(grids[gi].n))
+    launch_ms = per_grid_ms[gi] / args.steps / max(1, p.launches)
+    alg_bytes = 2 * S * ncell  # each launch reads and writes every cell once
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    fp_peak = {np.dtype(np.float32): capi.measure_fp_peak(np.float32),
+               np.dtype(np.float64): capi.measure_fp_peak(np.float64)}
+    per = []
+    for i, (nm, d_, n_, T_) in enumerate(work):
+        ms = per_grid_ms[i] / args.steps
+        gc = int(np.prod(grids[i].n)) * T_ / (ms * 1e-3) / 1e9
+        s = capi.info(nm)
+        Sb = np.dtype(d_).itemsize
+        bt = plans[i].bt
+        roof = min(hbm * 1e9 * bt / (2 * Sb), fp_peak[np.dtype(d_)] * 1e9 / s["fpp"]) / 1e9
+        roof1 = min(hbm * 1e9 / (2 * Sb), fp_peak[np.dtype(d_)] * 1e9 / s["fpp"]) / 1e9
+        per.append({"stencil": nm, "dtype": np.dtype(d_).name, "n": n_, "T": T_, "bt": bt,
+                    "launches": plans[i].launches, "ms": round(ms, 4), "gcells_s": round(gc, 2),
+                    "roofline_gcells_s": round(roof, 1), "frac_roofline": round(gc / roof, 4),
+                    "roofline_bt1_gcells_s": round(roof1, 1)})
+    launches = sum(p.launches for p in plans) * args.steps
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "+".join(sorted({np.dtype(w[1]).name.replace("float", "f") for w in work})),
+        "data": "synthetic U[0,1) grids and normalised U[0,1) coefficients, seeded",
+        "config": {"workload": args.workload, "grids": [f"{w[0]} {np.dtype(w[1]).name} {w[2]}^{capi.info(w[0])['dim']} T={w[3]}" for w in work],
+                   "fp_mode": args.fp_mode, "l2": "flushed between timed steps (512 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "per_stencil": per,
+        "e2e": {"value": round(cells * world / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GCells/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "kernel": f"{name} {np.dtype(dt).name} bt={p.bt}",
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"},
+        "fp_peak_gflops": {k.name: round(v, 1) for k, v in fp_peak.items()},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    return line
+
+
+# ---------------------------------------------------------------------------
+# CPU path (the artifact's OpenMP loop, restated bit for bit in oracle/)
+# ---------------------------------------------------------------------------
+def cpu_sample(work, budget_s=12.0, threads=None):
+    import pyoracle as po
+    if threads:
+        po.set_threads(threads)
+    cells, secs, parts = 0, 0.0, []
+    per_budget = budget_s / len(work)
+    for i, (name, dt, n, T) in enumerate(work):
+        A = np.empty((2,) + tuple([n + 2 * po.BY_NAME[name][1]["rad"]] * po.BY_NAME[name][1]["dim"]), dt)
+        rng = np.random.default_rng(20250101 + i)
+        A[0] = rng.random(A.shape[1:], dtype=np.float64 if dt == np.float64 else np.float32)
+        A[1] = A[0]
+        c = random_coefficients(name, dt, 1000 + i)
+        # one step to size the sample, then as many steps as fit the budget
+        ms1 = po.timed_run(name, A, n, 1, coef=c)
+        Ts = int(max(1, min(T, per_budget * 1e3 / max(ms1, 1e-3))))
+        ms = po.timed_run(name, A, n, Ts, coef=c)
+        ncell = n ** po.BY_NAME[name][1]["dim"]
+        cells += ncell * Ts
+        secs += ms * 1e-3
+        parts.append(f"{name} {np.dtype(dt).name} {n}^{po.BY_NAME[name][1]['dim']} T={Ts}")
+    return cells / secs / 1e9, "; ".join(parts)
+
+
+def run_reference(args, rank, world):
+    import pyoracle as po
+    work = WORKLOADS[args.workload]
+    threads = po.max_threads()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(work, budget_s=2.0)
+    sample = ""
+    for _ in range(args.steps):
+        v, sample = cpu_sample(work, budget_s=max(2.0, 60.0 / max(1, args.steps)))
+        vals.append(v)
+    value = statistics.median(vals)
+    return {
+        "metric": METRIC, "value": round(value, 4), "unit": "GCells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "impl": "reference",
+        "dtype": "+".join(sorted({np.dtype(w[1]).name.replace("float", "f") for w in work})),
+        "data": "synthetic U[0,1) grids and normalised U[0,1) coefficients, seeded",
+        "config": {"workload": args.workload, "grids": [f"{w[0]} {np.dtype(w[1]).name} {w[2]} T={w[3]}" for w in work]},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GCells/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "GCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="star2d1r", choices=sorted(WORKLOADS))
+    ap.add_argument("--fp-mode", default="fma", choices=["fma", "exact"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args, rank, world)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    line = run_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu:
+            import pyoracle as po
+            v, sample = cpu_sample(WORKLOADS[args.workload])
+            line["cpu_baseline"] = {"value": round(v, 4), "unit": "GCells/s", "cores": po.max_threads(),
+                                    "kind": "port", "sample": sample}
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

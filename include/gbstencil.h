@@ -132,6 +132,17 @@ gbs_status gbs_download(const gbs_desc *d, const void *dev_A, void *host_A, void
  * gave up) into GBS_ERR_TIMEOUT. */
 gbs_status gbs_sync(void *stream);
 
+/* Measures the device's fused multiply-add throughput in GFLOP/s (2 flops per
+ * FMA): the FP term of the temporally-blocked stencil roofline. */
+gbs_status gbs_measure_fp_peak(int dtype, double *gflops);
+
+/* Self-test of the engine's division by a constant divisor (used by j2d5pt,
+ * j2d9pt, j2d9pt-gol and j3d27pt) against IEEE division: float checks every
+ * one of the 2^32 inputs when samples <= 0; double checks `samples` random
+ * bit patterns (2^28 when samples <= 0) plus every binade edge.
+ * *mismatches receives the count of inputs whose results differ. */
+gbs_status gbs_check_division(int dtype, double divisor, long long samples, long long *mismatches);
+
 const char *gbs_last_error(void);
 /* Frees the cached device buffers of gbs_run. */
 void gbs_release_cache(void);

@@ -31,10 +31,11 @@ def max_class(name, dt, mode):
     if s["dim"] == 3:
         return 1
     if s["kind"] == "gradient":
-        return 8 if mode == "fma" else 2
+        return 2
+    cap = 8 if mode == "fma" else 4
     if s["form"] == "assoc":
-        return 8 if s["rad"] == 1 else (4 if s["rad"] == 2 else 2)
-    return 8 if s["rad"] <= 2 else 4
+        return cap if s["rad"] == 1 else (4 if s["rad"] == 2 else 2)
+    return cap if s["rad"] <= 2 else 4
 
 
 def random_grid(name, n, dt, seed):
