@@ -27,6 +27,13 @@ struct Geometry2D {
   int b, wout, nstrips, nblocks, sl;
 };
 
+struct Geometry3D {
+  int b, tj, jout, wk, ntk, ntj, nblocks, sl;
+};
+Geometry3D geometry3d(const Layout &L, int b, int sl_req, long long resident_ctas);
+gbs_status validate3d(const Layout &L, const Geometry3D &g);
+long long resident_ctas_3d(int sid, int dtype, int fma, int b);
+
 gbs_status fail(gbs_status st, const char *fmt, ...);
 gbs_status cuda_fail(cudaError_t e, const char *what);
 const gbs_stencil_def_t *stencil_def(int sid);

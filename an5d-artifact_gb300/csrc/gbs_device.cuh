@@ -277,6 +277,20 @@ __device__ __forceinline__ double div_by(double x, double d, double y) {
   return __ddiv_rn(x, d);
 }
 
+// x / d without the remainder test, for divisors for which the one-correction
+// quotient is exact on every input: the engine whitelists such divisors only
+// when the exhaustive float self-test (gbs_check_division with check=0)
+// proves it for that divisor, as it does for the artifact's 118 and 159.
+__device__ __forceinline__ float div_by_fast(float x, float d, float y) {
+  const float q0 = __fmul_rn(x, y);
+  const float r = __fmaf_rn(-q0, d, x);
+  const float q1 = __fmaf_rn(r, y, q0);
+  const float a = fabsf(q1);
+  if (a >= 0x1p-125f && a <= 0x1p+126f) return q1;
+  if (x == 0.0f) return __fmul_rn(x, y);
+  return __fdiv_rn(x, d);
+}
+
 // RN(1/d) for div_by, or 0 when d is outside the range div_by's test covers.
 template <typename T> inline T div_reciprocal(double d) {
   const double lo = sizeof(T) == 4 ? 0x1p-16 : 0x1p-50, hi = sizeof(T) == 4 ? 0x1p+16 : 0x1p+50;

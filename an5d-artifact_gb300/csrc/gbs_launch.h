@@ -14,6 +14,7 @@ struct Launch2D {
   int d0, d1, shift, b, wout, nstrips, nblocks, sl;
   const double *coef;
   double div, eps;
+  bool div_proven;    // the one-correction quotient is exact for every float input
 };
 
 // One launch of the 3-D family (see kernel3d.cuh).
@@ -21,21 +22,21 @@ struct Launch3D {
   const void *src;
   void *dst;
   int *err;
-  const void *tmap;   // device copy of the level-0 tensor map (64-byte aligned)
   long long pitch;    // elements per padded k-row
   int d0, d1, d2, shift, b;
-  int tj, wk;         // tile rows (warps) and valid k columns per tile
-  int jout;           // valid j rows per tile
+  int jout, wk;       // valid rows (j) and columns (k) per tile
   int ntk, ntj, nblocks, sl;
-  int src_plane;      // plane index the tensor map reads
   const double *coef;
-  double div, eps;
+  double div;
+  bool div_proven;
 };
 
 using Launch2DFn = cudaError_t (*)(const Launch2D &, cudaStream_t);
 // resident warps per SM of a 2-D launcher (occupancy), 0 on error
 using Occupancy2DFn = int (*)();
 using Launch3DFn = cudaError_t (*)(const Launch3D &, cudaStream_t);
+// resident CTAs per SM of a 3-D launcher (occupancy), 0 on error
+using Occupancy3DFn = int (*)();
 
 // Launchers of one (stencil, element type, fp mode), indexed by the fused
 // degree b (nullptr where none is built).
@@ -45,6 +46,7 @@ struct Picks {
   Launch2DFn l2[kMaxB + 1];
   Occupancy2DFn o2[kMaxB + 1];
   Launch3DFn l3[kMaxB + 1];
+  Occupancy3DFn o3[kMaxB + 1];
 };
 
 }  // namespace gbs

@@ -4,6 +4,7 @@
 // run the many units in parallel.
 #include "gbs_launch.h"
 #include "kernel2d.cuh"
+#include "kernel3d.cuh"
 
 #if !defined(GBS_SID) || !defined(GBS_T) || !defined(GBS_FMA) || !defined(GBS_PICK)
 #error "GBS_SID, GBS_T, GBS_FMA and GBS_PICK must be defined"
@@ -19,7 +20,8 @@ constexpr bool kFma = GBS_FMA != 0;
 // its 32*V columns to overlap, and stencils with many terms are FP-bound
 // before temporal blocking pays; FP64 on GB300 is FP-bound already at b=1.
 // Exact mode spends two FP instructions per term, so its best degree is
-// lower; it keeps degrees up to 4.
+// lower; it keeps degrees up to 4. In 3-D a tile of 32 rows loses 2*b*r rows
+// to overlap, and FP64 is compute-bound from b=1.
 constexpr int max_class() {
   if (S::kDim == 2) {
     if (sizeof(T) == 8) return 2;
@@ -28,7 +30,9 @@ constexpr int max_class() {
     if (S::kAssoc) return S::kRad == 1 ? cap : (S::kRad == 2 ? 4 : 2);
     return S::kRad <= 2 ? cap : 4;
   }
-  return 1;
+  if (S::kRad >= 3) return 1;
+  if (sizeof(T) == 8) return 2;
+  return S::kRad == 1 ? 4 : 3;
 }
 
 template <int B> void add(Picks &p) {
@@ -36,6 +40,9 @@ template <int B> void add(Picks &p) {
     if constexpr (S::kDim == 2) {
       p.l2[B] = &launch2d<S, T, B, kFma>;
       p.o2[B] = &occupancy2d<S, T, B, kFma>;
+    } else {
+      p.l3[B] = &launch3d<S, T, B, kFma>;
+      p.o3[B] = &occupancy3d<S, T, B, kFma>;
     }
     p.maxb = B;
   }

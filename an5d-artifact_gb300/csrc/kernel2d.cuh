@@ -53,7 +53,18 @@ template <typename T, int NT> struct Params2D {
   int nstrips, nblocks, sl;
   T coef[NT];
   T div, rdiv, eps;    // divisor, RN(1/divisor), gradient epsilon
+  int divmode;         // 0: no division (folded into coef), 1: checked, 2: proven fast path
 };
+
+// y / div as the params ask (see div_by / div_by_fast)
+template <typename T, int NT>
+__device__ __forceinline__ T apply_div(T y, const Params2D<T, NT> &p) {
+  if constexpr (sizeof(T) == 4) {
+    if (p.divmode == 2) return div_by_fast(y, p.div, p.rdiv);
+  }
+  if (p.divmode == 0) return y;
+  return div_by(y, p.div, p.rdiv);
+}
 
 // Compile-time facts about a stencil's term list.
 template <class ST, int V> struct Tap2 {
@@ -150,7 +161,7 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
         });
         if constexpr (ST::kHasDiv) {
 #pragma unroll
-          for (int e = 0; e < V; ++e) y[e] = div_by(y[e], p.div, p.rdiv);
+          for (int e = 0; e < V; ++e) y[e] = apply_div(y[e], p);
         }
       }
       if (CAREFUL && edge) {
@@ -187,7 +198,7 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
     for (int e = 0; e < V; ++e) y[e] = win[oslot][e];
     if constexpr (ST::kHasDiv) {
 #pragma unroll
-      for (int e = 0; e < V; ++e) y[e] = div_by(y[e], p.div, p.rdiv);
+      for (int e = 0; e < V; ++e) y[e] = apply_div(y[e], p);
     }
     if constexpr (CAREFUL) {
       if (halo_row) {
@@ -387,7 +398,10 @@ cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
   p.nstrips = a.nstrips;
   p.nblocks = a.nblocks;
   p.sl = a.sl;
-  for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = (T)a.coef[t];
+  // FMA mode is tolerance-bound: a divisor is folded into the coefficients
+  const bool fold = FMA && ST::kHasDiv && a.div != 0.0;
+  for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = fold ? (T)(a.coef[t] / a.div) : (T)a.coef[t];
+  p.divmode = !ST::kHasDiv || fold ? 0 : (a.div_proven ? 2 : 1);
   p.div = (T)a.div;
   p.rdiv = div_reciprocal<T>(a.div);
   p.eps = (T)a.eps;

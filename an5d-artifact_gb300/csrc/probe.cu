@@ -80,12 +80,12 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   return z ^ (z >> 31);
 }
 
-__global__ void div_check_f32(float d, float y, unsigned long long count, unsigned long long *mism) {
+__global__ void div_check_f32(float d, float y, int fast, unsigned long long count, unsigned long long *mism) {
   unsigned long long bad = 0;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
     const float x = __uint_as_float((unsigned)i);
-    const float a = gbs::div_by(x, d, y), b = __fdiv_rn(x, d);
+    const float a = fast ? gbs::div_by_fast(x, d, y) : gbs::div_by(x, d, y), b = __fdiv_rn(x, d);
     if (__float_as_uint(a) != __float_as_uint(b) && !(isnan(a) && isnan(b))) ++bad;
   }
   if (bad) atomicAdd(mism, bad);
@@ -108,7 +108,8 @@ __global__ void div_check_f64(double d, double y, unsigned long long count, unsi
 }
 }  // namespace
 
-extern "C" gbs_status gbs_check_division(int dtype, double divisor, long long samples, long long *mismatches) {
+extern "C" gbs_status gbs_check_division(int dtype, double divisor, int checked, long long samples,
+                                         long long *mismatches) {
   if (!mismatches) return gbs::fail(GBS_ERR_INVALID, "mismatches is NULL");
   if (divisor == 0.0) return gbs::fail(GBS_ERR_INVALID, "divisor must be nonzero");
   unsigned long long *m = nullptr;
@@ -121,7 +122,7 @@ extern "C" gbs_status gbs_check_division(int dtype, double divisor, long long sa
   if (dtype == GBS_F32) {
     const float d = (float)divisor, y = gbs::div_reciprocal<float>(divisor);
     const unsigned long long count = samples > 0 ? (unsigned long long)samples : (1ull << 32);
-    div_check_f32<<<sms * 8, 256>>>(d, y, count, m);
+    div_check_f32<<<sms * 8, 256>>>(d, y, checked ? 0 : 1, count, m);
   } else if (dtype == GBS_F64) {
     const double y = gbs::div_reciprocal<double>(divisor);
     const unsigned long long count = samples > 0 ? (unsigned long long)samples : (1ull << 28);

@@ -67,7 +67,7 @@ SIGNATURES = [
     ("gbs_download", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_sync", ctypes.c_int, [ctypes.c_void_p]),
     ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
-    ("gbs_check_division", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_longlong,
+    ("gbs_check_division", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_longlong,
                                           ctypes.POINTER(ctypes.c_longlong)]),
     ("gbs_last_error", ctypes.c_char_p, []),
     ("gbs_release_cache", None, []),
@@ -180,12 +180,12 @@ def measure_fp_peak(dtype) -> float:
     return g.value
 
 
-def check_division(dtype, divisor: float, samples: int = 0) -> int:
+def check_division(dtype, divisor: float, samples: int = 0, checked: bool = True) -> int:
     """Inputs on which the engine's constant-divisor division differs from
     IEEE division (see gbs_check_division)."""
     m = ctypes.c_longlong(-1)
     dt = GBS_F32 if np.dtype(dtype) == np.float32 else GBS_F64
-    check(lib().gbs_check_division(dt, float(divisor), int(samples), ctypes.byref(m)))
+    check(lib().gbs_check_division(dt, float(divisor), int(bool(checked)), int(samples), ctypes.byref(m)))
     return m.value
 
 

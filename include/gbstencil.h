@@ -137,11 +137,15 @@ gbs_status gbs_sync(void *stream);
 gbs_status gbs_measure_fp_peak(int dtype, double *gflops);
 
 /* Self-test of the engine's division by a constant divisor (used by j2d5pt,
- * j2d9pt, j2d9pt-gol and j3d27pt) against IEEE division: float checks every
- * one of the 2^32 inputs when samples <= 0; double checks `samples` random
- * bit patterns (2^28 when samples <= 0) plus every binade edge.
- * *mismatches receives the count of inputs whose results differ. */
-gbs_status gbs_check_division(int dtype, double divisor, long long samples, long long *mismatches);
+ * j2d9pt, j2d9pt-gol and j3d27pt in GBS_FP_EXACT mode) against IEEE
+ * division. checked != 0 tests the remainder-checked quotient used for any
+ * divisor; checked == 0 tests the unchecked one-correction quotient that the
+ * engine uses only for divisors this test proves exact (118 and 159). Float
+ * checks every one of the 2^32 inputs when samples <= 0; double checks
+ * `samples` random bit patterns (2^28 when samples <= 0) plus every binade
+ * edge. *mismatches receives the count of inputs whose results differ. */
+gbs_status gbs_check_division(int dtype, double divisor, int checked, long long samples,
+                              long long *mismatches);
 
 const char *gbs_last_error(void);
 /* Frees the cached device buffers of gbs_run. */

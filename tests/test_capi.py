@@ -71,7 +71,7 @@ def test_layout_invariants(name, dt, n):
 def test_plan_final_plane_parity(T, bt):
     """Launch j reads plane j%2; the result must land in plane T%2, so the
     number of launches must have the parity of T."""
-    d, _ = capi.make_desc("star2d1r", np.float32, 64, T, bt=bt)
+    d, _ = capi.make_desc("star2d1r", np.float32, 64, T, fp_mode="fma", bt=bt)
     p = capi.plan(d)
     assert p.launches % 2 == T % 2
     assert p.launches >= -(-T // bt)

@@ -26,10 +26,14 @@ NAMES_3D = [s["name"] for s in capi.TABLE if s["dim"] == 3]
 def max_class(name, dt, mode):
     """Largest fused degree the build instantiates (mirrors csrc/inst.cu)."""
     s = capi.info(name)
+    if s["dim"] == 3:
+        if s["rad"] >= 3:
+            return 1
+        if np.dtype(dt) == np.float64:
+            return 2
+        return 4 if s["rad"] == 1 else 3
     if np.dtype(dt) == np.float64:
         return 2
-    if s["dim"] == 3:
-        return 1
     if s["kind"] == "gradient":
         return 2
     cap = 8 if mode == "fma" else 4
@@ -116,7 +120,7 @@ def test_parity_2d_random_coefficients(name):
     compare(name, A0, nn, 20, np.float32, "exact", 4, coef=c)
 
 
-@pytest.mark.parametrize("case", [c for c in GOLDEN if c["stencil"] in NAMES_2D],
+@pytest.mark.parametrize("case", GOLDEN,
                          ids=lambda c: f"{c['stencil']}-{c['dtype']}-{c['compsize']}-{c['timestep']}")
 def test_exact_mode_matches_artifact_golden(case):
     """Bit-identical to the artifact's own CPU path (committed digests)."""
@@ -126,3 +130,30 @@ def test_exact_mode_matches_artifact_golden(case):
     d, _ = capi.make_desc(name, dt, n, T, fp_mode="exact")
     capi.run_host(d, A)
     assert hashlib.sha256(np.ascontiguousarray(A[T % 2]).tobytes()).hexdigest() == case["sha256"]
+
+
+CASES_3D = [  # (n, T, sl)
+    (11, 1, 0), (11, 2, 0), (20, 3, 0), ((13, 40, 150), 4, 0), (70, 3, 9), ((37, 9, 300), 5, 0),
+]
+
+
+@pytest.mark.parametrize("mode", ["exact", "fma"])
+@pytest.mark.parametrize("dt", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("name", NAMES_3D)
+def test_parity_3d(name, dt, mode):
+    mc = max_class(name, dt, mode)
+    seed = 100
+    for n, T, sl in CASES_3D:
+        for bt in sorted({1, mc, 2 if mc >= 2 else 1}):
+            seed += 1
+            A0, nn = random_grid(name, n, dt, seed)
+            compare(name, A0, nn, T, dt, mode, bt, sl=sl)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("name", NAMES_3D)
+def test_parity_3d_reference_init(name, dt):
+    n, T = 40, 5
+    A0 = po.init_grid(name, n, dt)
+    compare(name, A0, [n, n, n], T, dt, "exact", max_class(name, dt, "exact"))
+    compare(name, A0, [n, n, n], T, dt, "fma", max_class(name, dt, "fma"))
