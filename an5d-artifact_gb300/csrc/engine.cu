@@ -39,6 +39,8 @@ gbs_status fail(gbs_status st, const char *fmt, ...) {
 }
 
 gbs_status cuda_fail(cudaError_t e, const char *what) {
+  // leave no non-sticky error behind for the caller's next CUDA call
+  (void)cudaGetLastError();
   if (e == cudaErrorMemoryAllocation)
     return fail(GBS_ERR_NOMEM, "%s: %s", what, cudaGetErrorString(e));
   return fail(GBS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));

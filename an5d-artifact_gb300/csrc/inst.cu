@@ -31,8 +31,10 @@ constexpr int max_class() {
     return S::kRad <= 2 ? cap : 4;
   }
   if (S::kRad >= 3) return 1;
-  if (sizeof(T) == 8) return 2;
-  return S::kRad == 1 ? 4 : 3;
+  int b = sizeof(T) == 8 ? 2 : (S::kRad == 1 ? 4 : 3);
+  // the level rings must fit the 227 KB of shared memory a CTA may use
+  while (b > 1 && Smem3<S, T, kFma>::bytes(kTj3D, b) > 227u * 1024u) --b;
+  return b;
 }
 
 template <int B> void add(Picks &p) {

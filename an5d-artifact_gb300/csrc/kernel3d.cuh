@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(TJ * 32, 1)
         in_q = ring0 + (size_t)(((q - pstart) % NS + NS) % NS) * PLANE;
       } else {
         const T *rl = rings + (size_t)(l - 1) * DEP * PLANE;
-        in_m = rl + (size_t)((s - 1) % DEP) * PLANE;
+        in_m = rl + (size_t)(((s - 1) % DEP + DEP) % DEP) * PLANE;
         in_q = rl + (size_t)(((s - 1 - R) % DEP + DEP) % DEP) * PLANE;
       }
       const bool qhalo = (q < R || q >= p.d0 - R);
@@ -409,7 +409,10 @@ cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return e;
+    }
     attr_set = true;
   }
   Params3D<T, ST::kTerms> p;

@@ -31,6 +31,8 @@ def max_class(name, dt, mode):
             return 1
         if np.dtype(dt) == np.float64:
             return 2
+        if mode == "exact" and s["form"] == "direct" and s["rad"] == 2:
+            return 2  # shared-memory bound of the direct form's plane rings
         return 4 if s["rad"] == 1 else 3
     if np.dtype(dt) == np.float64:
         return 2
