@@ -222,11 +222,16 @@ long long resident_ctas_3d(int sid, int dtype, int fma, int b) {
 // Tiles of 32 rows x one 32*V-column window; the number of stream blocks is
 // chosen to fill whole waves of resident CTAs while keeping the 2*b*r-plane
 // stream overlap small.
-Geometry3D geometry3d(const Layout &L, int b, int sl_req, long long resident) {
+int tile_rows_3d(int sid, int dtype, int fma, int b) {
+  const Picks &pk = picks(sid, dtype, fma);
+  return (b <= kMaxB && pk.tj3[b] > 0) ? pk.tj3[b] : 32;
+}
+
+Geometry3D geometry3d(const Layout &L, int b, int tj, int sl_req, long long resident) {
   Geometry3D g{};
   const int R = L.rad, V = L.V;
   g.b = b;
-  g.tj = 32;
+  g.tj = tj;
   g.jout = g.tj - 2 * b * R;
   g.wk = ((32 * V - 2 * b * R - (V - 1)) / V) * V;
   const int ni = L.dims[0] - 2 * R, nj = L.dims[1] - 2 * R, nk = L.dims[2] - 2 * R;
@@ -257,7 +262,8 @@ Geometry3D geometry3d(const Layout &L, int b, int sl_req, long long resident) {
 gbs_status validate3d(const Layout &L, const Geometry3D &g) {
   const int R = L.rad, V = L.V, ROW = 32 * V;
   if (g.jout <= 0 || g.wk <= 0)
-    return fail(GBS_ERR_UNSUPPORTED, "fused degree %d leaves no output cells in a 32-row tile (r=%d)", g.b, R);
+    return fail(GBS_ERR_UNSUPPORTED, "fused degree %d leaves no output cells in a %d-row tile (r=%d)", g.b,
+                g.tj, R);
   if ((L.pitch * (long long)L.esize) % 16 != 0) return fail(GBS_ERR_INVALID, "internal: pitch alignment");
   for (int t = 0; t < g.ntk; ++t) {
     const int cs = R + t * g.wk;
@@ -393,7 +399,8 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
       cudaError_t e = pk.l2[b](a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");
     } else {
-      Geometry3D g = geometry3d(L, b, d->sl, resident_ctas_3d(d->stencil, d->dtype, fma, b));
+      Geometry3D g = geometry3d(L, b, tile_rows_3d(d->stencil, d->dtype, fma, b), d->sl,
+                                 resident_ctas_3d(d->stencil, d->dtype, fma, b));
       gbs_status st = validate3d(L, g);
       if (st != GBS_OK) return st;
       Launch3D a{};
@@ -496,7 +503,8 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
     const double cols = 32.0 * L.V, rows = g.sl + 2.0 * bt * L.rad;
     out->redundancy = (cols * rows) / ((double)g.wout * g.sl);
   } else {
-    Geometry3D g = geometry3d(L, bt, d->sl, resident_ctas_3d(d->stencil, d->dtype, fma, bt));
+    Geometry3D g = geometry3d(L, bt, tile_rows_3d(d->stencil, d->dtype, fma, bt), d->sl,
+                                 resident_ctas_3d(d->stencil, d->dtype, fma, bt));
     st = validate3d(L, g);
     if (st != GBS_OK) return st;
     out->bs1 = g.tj;

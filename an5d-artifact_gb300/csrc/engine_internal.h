@@ -30,7 +30,8 @@ struct Geometry2D {
 struct Geometry3D {
   int b, tj, jout, wk, ntk, ntj, nblocks, sl;
 };
-Geometry3D geometry3d(const Layout &L, int b, int sl_req, long long resident_ctas);
+Geometry3D geometry3d(const Layout &L, int b, int tj, int sl_req, long long resident_ctas);
+int tile_rows_3d(int sid, int dtype, int fma, int b);
 gbs_status validate3d(const Layout &L, const Geometry3D &g);
 long long resident_ctas_3d(int sid, int dtype, int fma, int b);
 

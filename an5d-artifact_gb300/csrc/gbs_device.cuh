@@ -165,6 +165,13 @@ __device__ __forceinline__ T row_elem(const T (&row)[V]) {
   }
 }
 
+// Window slots: with UNR the loop over pipeline steps is unrolled W times and
+// the logical window position j (0 = oldest row/plane) of phase ph lives in
+// slot (ph + 1 + j) % W, so the window rotates by renaming; without UNR
+// (to keep the code small) slot == j and the window shifts by moves.
+template <bool UNR, int W>
+__host__ __device__ constexpr int wslot(int ph, int j) { return UNR ? (ph + 1 + j) % W : j; }
+
 // ---- arithmetic modes ---------------------------------------------------------
 // Exact mode: products and sums rounded separately (never contracted).
 // FMA mode: acc + c*a as one fused operation.

@@ -47,6 +47,7 @@ struct Picks {
   Occupancy2DFn o2[kMaxB + 1];
   Launch3DFn l3[kMaxB + 1];
   Occupancy3DFn o3[kMaxB + 1];
+  int tj3[kMaxB + 1];   // tile rows of the 3-D launcher
 };
 
 }  // namespace gbs

@@ -19,6 +19,22 @@ constexpr bool kFma = GBS_FMA != 0;
 // Fused-degree classes worth instantiating. A b-level strip loses 2*b*r of
 // its 32*V columns to overlap, and stencils with many terms are FP-bound
 // before temporal blocking pays; FP64 on GB300 is FP-bound already at b=1.
+// shared memory and tile rows of the 3-D launcher of degree b (run time b)
+template <int... Bs>
+constexpr size_t smem_pick(int b, std::integer_sequence<int, Bs...>) {
+  size_t r = 0;
+  ((r = (Bs + 1 == b) ? smem_bytes3d<S, T, Bs + 1, kFma>() : r), ...);
+  return r;
+}
+template <int... Bs>
+constexpr int rows_pick(int b, std::integer_sequence<int, Bs...>) {
+  int r = 0;
+  ((r = (Bs + 1 == b) ? tile_rows3d<S, T, Bs + 1, kFma>() : r), ...);
+  return r;
+}
+constexpr size_t smem_bytes3d_b(int b) { return smem_pick(b, std::make_integer_sequence<int, 4>()); }
+constexpr int tile_rows_b(int b) { return rows_pick(b, std::make_integer_sequence<int, 4>()); }
+
 // Exact mode spends two FP instructions per term, so its best degree is
 // lower; it keeps degrees up to 4. In 3-D a tile of 32 rows loses 2*b*r rows
 // to overlap, and FP64 is compute-bound from b=1.
@@ -33,7 +49,7 @@ constexpr int max_class() {
   if (S::kRad >= 3) return 1;
   int b = sizeof(T) == 8 ? 2 : (S::kRad == 1 ? 4 : 3);
   // the level rings must fit the 227 KB of shared memory a CTA may use
-  while (b > 1 && Smem3<S, T, kFma>::bytes(kTj3D, b) > 227u * 1024u) --b;
+  while (b > 1 && (smem_bytes3d_b(b) > 227u * 1024u || tile_rows_b(b) <= 2 * b * S::kRad)) --b;
   return b;
 }
 
@@ -45,6 +61,7 @@ template <int B> void add(Picks &p) {
     } else {
       p.l3[B] = &launch3d<S, T, B, kFma>;
       p.o3[B] = &occupancy3d<S, T, B, kFma>;
+      p.tj3[B] = tile_rows3d<S, T, B, kFma>();
     }
     p.maxb = B;
   }

@@ -99,12 +99,6 @@ __device__ __forceinline__ void extend_row(T (&ext)[V + 2 * ST::kRad], const T (
   });
 }
 
-// Window slots: with UNR the loop over pipeline steps is unrolled W times and
-// the logical window position j (0 = oldest row) of phase ph lives in slot
-// (ph + 1 + j) % W, so the window rotates by renaming; without UNR (large
-// radii, to keep the code small) slot == j and the window shifts by moves.
-template <bool UNR, int W>
-__host__ __device__ constexpr int wslot(int ph, int j) { return UNR ? (ph + 1 + j) % W : j; }
 
 // One fused time level: the level-(l) row x arrives, the level-(l+1) row q
 // leaves in x. CAREFUL handles halo rows and columns (grid edges);
@@ -152,12 +146,14 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
           constexpr int t = decltype(TI)::value;
           constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
           constexpr int slot = wslot<UNR, W>(PH, R + di);
-#pragma unroll
-          for (int e = 0; e < V; ++e) {
-            const T a = (dj == 0) ? win[slot][e] : ext[di + R][R + e + dj];
+          static_for<V>([&](auto EI) {
+            constexpr int e = decltype(EI)::value;
+            T a;
+            if constexpr (dj == 0) a = win[slot][e];
+            else a = ext[di + R][R + e + dj];
             if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
             else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
-          }
+          });
         });
         if constexpr (ST::kHasDiv) {
 #pragma unroll
@@ -186,12 +182,12 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
       constexpr int t = decltype(TI)::value;
       constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
       constexpr int slot = wslot<UNR, W>(PH, R - di);
-#pragma unroll
-      for (int e = 0; e < V; ++e) {
+      static_for<V>([&](auto EI) {
+        constexpr int e = decltype(EI)::value;
         const T a = ext[R + e + dj];
         if constexpr (t == 0) win[slot][e] = A::mul(p.coef[t], a);
         else win[slot][e] = term_next<T, FMA>(win[slot][e], p.coef[t], a);
-      }
+      });
     });
     constexpr int oslot = wslot<UNR, W>(PH, 0);
 #pragma unroll
