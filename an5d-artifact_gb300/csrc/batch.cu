@@ -1,0 +1,410 @@
+// Batched persistent launch: many independent 2-D grids of uneven sizes,
+// radii and step counts advanced by ONE kernel launch, replayed from a CUDA
+// graph.
+//
+// Work items are (grid, time block, strip, stream block): one warp runs the
+// same temporally-blocked pipeline as the single-grid kernel
+// (warp_item2d) on one item. The host orders the items by time block;
+// persistent warps take them in that order from an atomic counter. An item
+// of time block k of grid g starts once every item of g's earlier blocks has
+// finished (a per-grid completion counter reaching the item's `need`). The
+// order makes this deadlock-free: every item an item waits on was taken
+// earlier by a running warp that never waits on a later item. Waits are
+// bounded (the error word is set and the warp stops).
+//
+// Memory ordering: a finishing item's lanes fence their stores, then lane 0
+// increments the grid's counter; a starting item's lane 0 reads the counter
+// with acquire semantics and issues a proxy fence before its bulk copies (an
+// async-proxy read) touch the data. Loads outside the bulk copies bypass L1.
+//
+// Built twice: -DGBS_FMA=0 (exact mode) and -DGBS_FMA=1.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "engine_internal.h"
+#include "kernel2d.cuh"
+
+#ifndef GBS_FMA
+#error "GBS_FMA must be defined"
+#endif
+
+namespace gbs {
+namespace batchdetail {
+constexpr int kMaxTerms = 81;
+
+struct GridDev {
+  float *base;          // two-plane buffer (engine layout)
+  long long pitch, plane;
+  int d0, d1, shift, sid;
+  int sl, nblocks;
+  float coef[kMaxTerms];
+  float div, rdiv, eps;
+  int divmode;
+};
+
+struct Item {
+  int grid, k, b, strip, blk, need, pad0, pad1;
+};
+}  // namespace batchdetail
+using batchdetail::GridDev;
+using batchdetail::Item;
+
+namespace {
+constexpr bool kFma = GBS_FMA != 0;
+constexpr int kWpc = kWpc2D, kStages = kStages2D;
+
+// The stencils a batch may mix and the fused degree used for each (the full
+// blocks; remainders run at degree 1).
+template <class S> constexpr int batch_degree() {
+  if (S::kKind == KIND_GRADIENT) return 1;
+  if (S::kRad == 1) return S::kAssoc ? 4 : 4;
+  if (S::kRad == 2) return 2;
+  if (S::kRad == 3) return S::kAssoc ? 1 : 2;
+  return 1;
+}
+
+struct Args {
+  const GridDev *grids;
+  const Item *items;
+  int nitems;
+  unsigned *next;       // work counter
+  unsigned *done;       // per-grid completed items
+  int *err;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <class S, int B>
+__device__ __forceinline__ bool run_item(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
+                                         unsigned &load_base, int *err) {
+  Params2D<float, S::kTerms> p;
+  p.src = g.base + (long long)(it.k % 2) * g.plane;
+  p.dst = g.base + (long long)((it.k + 1) % 2) * g.plane;
+  p.err = err;
+  p.pitch = g.pitch;
+  p.d0 = g.d0;
+  p.d1 = g.d1;
+  p.shift = g.shift;
+  p.b = B;
+  p.wout = ((128 - 2 * B * S::kRad - 3) / 4) * 4;
+  p.nstrips = 0;
+  p.nblocks = g.nblocks;
+  p.sl = g.sl;
+#pragma unroll
+  for (int t = 0; t < S::kTerms; ++t) p.coef[t] = g.coef[t];
+  p.div = g.div;
+  p.rdiv = g.rdiv;
+  p.eps = g.eps;
+  p.divmode = g.divmode;
+  return warp_item2d<S, float, B, kFma, kStages>(p, it.strip, it.blk, ring, bars, load_base);
+}
+
+template <class S>
+__device__ __forceinline__ bool dispatch_b(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
+                                           unsigned &load_base, int *err) {
+  constexpr int BS = batch_degree<S>();
+  if (it.b == BS) return run_item<S, BS>(g, it, ring, bars, load_base, err);
+  if constexpr (BS != 1) {
+    if (it.b == 1) return run_item<S, 1>(g, it, ring, bars, load_base, err);
+  }
+  return false;
+}
+
+__device__ bool dispatch(const GridDev &g, const Item &it, float *ring, uint64_t *bars, unsigned &load_base,
+                         int *err) {
+  switch (g.sid) {
+#define GBS_CASE(id, S)                                                  \
+  case id:                                                               \
+    if constexpr (S::kDim == 2)                                          \
+      return dispatch_b<S>(g, it, ring, bars, load_base, err);           \
+    else                                                                 \
+      return false;
+    GBS_FOR_EACH_STENCIL(GBS_CASE)
+#undef GBS_CASE
+    default:
+      return false;
+  }
+}
+
+__global__ void __launch_bounds__(kWpc * 32, 4) batch2d_kernel(const __grid_constant__ Args a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float *ring;
+  uint64_t *bars;
+  warp_ring2d<float, kWpc, kStages>(smem_raw, ring, bars);
+  const int lane = threadIdx.x & 31;
+  unsigned load_base = 0;
+  while (true) {
+    unsigned idx = 0;
+    if (lane == 0) idx = atomicAdd(a.next, 1u);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= (unsigned)a.nitems) break;
+    const Item it = a.items[idx];
+    bool ok = true;
+    if (lane == 0 && it.need > 0) {
+      const unsigned long long t0 = global_ns();
+      unsigned spins = 0;
+      while (ld_acquire(&a.done[it.grid]) < (unsigned)it.need) {
+        if (++spins > 64) {
+          __nanosleep(200);
+          if (global_ns() - t0 > kWaitLimitNs) {
+            atomicOr(a.err, ERR_DEP_TIMEOUT);
+            ok = false;
+            break;
+          }
+        }
+      }
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
+    if (!__all_sync(0xffffffffu, ok)) break;
+    __syncwarp();
+    if (!dispatch(a.grids[it.grid], it, ring, bars, load_base, a.err)) {
+      if (lane == 0) atomicOr(a.err, ERR_WAIT_TIMEOUT);
+      break;
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) atomicAdd(&a.done[it.grid], 1u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int family_degree(int sid) {
+  switch (sid) {
+#define GBS_DEG(id, S) \
+  case id:             \
+    return S::kDim == 2 ? batch_degree<S>() : 0;
+    GBS_FOR_EACH_STENCIL(GBS_DEG)
+#undef GBS_DEG
+    default:
+      return 0;
+  }
+}
+
+// time blocks of T steps: blocks of degree bs plus single steps, with as
+// many blocks as T has parity (launch k reads plane k%2)
+std::vector<int> batch_blocks(int T, int bs) {
+  std::vector<int> out;
+  if (T <= 0) return out;
+  int n = T / bs, r = T - n * bs;
+  if (((n + r) - T) % 2 != 0) {  // only possible for even bs
+    if (n > 0) {
+      --n;
+      r += bs;
+    }
+  }
+  for (int i = 0; i < n; ++i) out.push_back(bs);
+  for (int i = 0; i < r; ++i) out.push_back(1);
+  return out;
+}
+}  // namespace
+}  // namespace gbs
+
+using namespace gbs;
+
+struct gbs_batch {
+  gbs::batchdetail::GridDev *d_grids = nullptr;
+  gbs::batchdetail::Item *d_items = nullptr;
+  unsigned *d_counters = nullptr;  // [0] next, [1..] done per grid
+  int ngrids = 0, nitems = 0, ctas = 0;
+  long long cells = 0;             // sum over grids of interior cells * timestep
+  size_t smem = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int launches_plain = 0;          // what per-grid plain launches would need
+};
+
+#define GBS_BATCH_FN(name) GBS_BATCH_FN2(name, GBS_FMA)
+#define GBS_BATCH_FN2(name, m) GBS_BATCH_FN3(name, m)
+#define GBS_BATCH_FN3(name, m) name##_##m
+
+extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grids, int ngrids, gbs_batch **out) {
+  if (!grids || ngrids <= 0 || !out) return fail(GBS_ERR_INVALID, "batch: no grids");
+  std::vector<GridDev> gd(ngrids);
+  std::vector<std::vector<int>> blocks(ngrids);
+  long long cells = 0;
+  for (int g = 0; g < ngrids; ++g) {
+    const gbs_batch_grid &bg = grids[g];
+    const gbs_stencil_def_t *s = stencil_def(bg.stencil);
+    if (!s || s->dim != 2) return fail(GBS_ERR_INVALID, "batch grid %d: not a 2-D stencil", g);
+    if (bg.n[0] < 1 || bg.n[1] < 1 || bg.timestep < 0 || !bg.dev_A)
+      return fail(GBS_ERR_INVALID, "batch grid %d: bad extent, timestep or buffer", g);
+    if (reinterpret_cast<uintptr_t>(bg.dev_A) % 128 != 0)
+      return fail(GBS_ERR_INVALID, "batch grid %d: buffer not 128-byte aligned", g);
+    gbs_desc d{};
+    d.stencil = bg.stencil;
+    d.dtype = GBS_F32;
+    d.n[0] = bg.n[0];
+    d.n[1] = bg.n[1];
+    d.n[2] = 1;
+    d.timestep = bg.timestep;
+    d.fp_mode = kFma ? GBS_FP_FMA : GBS_FP_EXACT;
+    const Layout L = make_layout(&d);
+    GridDev &x = gd[g];
+    std::memset(&x, 0, sizeof x);
+    x.base = static_cast<float *>(bg.dev_A);
+    x.pitch = L.pitch;
+    x.plane = L.plane;
+    x.d0 = L.dims[0];
+    x.d1 = L.dims[1];
+    x.shift = (int)L.shift;
+    x.sid = bg.stencil;
+    const int ni = L.dims[0] - 2 * s->rad;
+    // stream blocks of about 128 rows keep items short for load balance
+    x.sl = std::min(ni, std::max(32, (ni + 7) / 8 > 128 ? 128 : (ni + 7) / 8 < 32 ? 32 : (ni + 7) / 8));
+    x.nblocks = (ni + x.sl - 1) / x.sl;
+    const double div = bg.divisor != 0.0 ? bg.divisor : (double)s->divisor;
+    const bool fold = kFma && s->divisor && div != 0.0;
+    const int nt = s->kind == 1 ? 1 : s->nterms;
+    for (int t = 0; t < nt; ++t) {
+      double c = bg.coef ? (double)((const float *)bg.coef)[t]
+                         : (s->kind == 1 ? (double)s->numerator : (double)s->terms[t].coef);
+      x.coef[t] = fold ? (float)(c / div) : (float)c;
+    }
+    x.div = (float)div;
+    x.rdiv = div_reciprocal<float>(div);
+    x.eps = (float)s->eps;
+    x.divmode = !s->divisor || fold ? 0 : (div_proven_exact(div) ? 2 : 1);
+    blocks[g] = batch_blocks(bg.timestep, family_degree(bg.stencil));
+    cells += (long long)bg.n[0] * bg.n[1] * bg.timestep;
+    // validate every strip window of every degree used
+    for (int b : blocks[g]) {
+      Geometry2D geo = geometry2d(L, b, x.sl, 0);
+      gbs_status st = validate2d(L, geo);
+      if (st != GBS_OK) return st;
+    }
+  }
+  // items ordered by time block, grids interleaved within a block
+  std::vector<Item> items;
+  std::vector<int> done_before(ngrids, 0);
+  size_t kmax = 0;
+  for (auto &b : blocks) kmax = std::max(kmax, b.size());
+  for (size_t k = 0; k < kmax; ++k) {
+    for (int g = 0; g < ngrids; ++g) {
+      if (k >= blocks[g].size()) continue;
+      const int b = blocks[g][k];
+      const gbs_stencil_def_t *s = stencil_def(grids[g].stencil);
+      const int wout = ((128 - 2 * b * s->rad - 3) / 4) * 4;
+      const int nj = gd[g].d1 - 2 * s->rad;
+      const int nstrips = (nj + wout - 1) / wout;
+      const int need = done_before[g];
+      for (int blk = 0; blk < gd[g].nblocks; ++blk)
+        for (int st = 0; st < nstrips; ++st) items.push_back(Item{g, (int)k, b, st, blk, need, 0, 0});
+      done_before[g] += nstrips * gd[g].nblocks;
+    }
+  }
+  auto *h = new gbs_batch();
+  h->ngrids = ngrids;
+  h->nitems = (int)items.size();
+  h->cells = cells;
+  for (auto &b : blocks) h->launches_plain += (int)b.size();
+  cudaError_t e;
+  if ((e = cudaMalloc(&h->d_grids, sizeof(GridDev) * ngrids)) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_items, sizeof(Item) * std::max<size_t>(1, items.size()))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_counters, sizeof(unsigned) * (ngrids + 1))) != cudaSuccess) {
+    gbs_batch_destroy(h);
+    return cuda_fail(e, "batch: cudaMalloc");
+  }
+  cudaMemcpy(h->d_grids, gd.data(), sizeof(GridDev) * ngrids, cudaMemcpyHostToDevice);
+  if (!items.empty()) cudaMemcpy(h->d_items, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice);
+  int *err = nullptr;
+  gbs_status st = error_word(&err);
+  if (st != GBS_OK) {
+    gbs_batch_destroy(h);
+    return st;
+  }
+  h->smem = (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t));
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch2d_kernel, kWpc * 32, h->smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  (void)cudaGetLastError();
+  // every CTA resident at once (persistent), never more CTAs than warps of work
+  h->ctas = std::max(1, std::min(per_sm * sms, (h->nitems + kWpc - 1) / kWpc));
+
+  Args a{};
+  a.grids = h->d_grids;
+  a.items = h->d_items;
+  a.nitems = h->nitems;
+  a.next = h->d_counters;
+  a.done = h->d_counters + 1;
+  a.err = err;
+  // capture: reset the counters, then the persistent kernel
+  cudaStream_t cs;
+  if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) {
+    gbs_batch_destroy(h);
+    return cuda_fail(e, "batch: stream");
+  }
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned) * (ngrids + 1), cs);
+    batch2d_kernel<<<h->ctas, kWpc * 32, h->smem, cs>>>(a);
+    e = cudaStreamEndCapture(cs, &h->graph);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&h->exec, h->graph, 0);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    gbs_batch_destroy(h);
+    return cuda_fail(e, "batch: graph capture");
+  }
+  *out = h;
+  return GBS_OK;
+}
+
+#if GBS_FMA
+// The C ABI entry points live in the FMA unit; they dispatch on fp_mode.
+extern "C++" gbs_status gbs_batch_build_0(const gbs_batch_grid *, int, gbs_batch **);
+
+extern "C" {
+gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, gbs_batch **out) {
+  if (dtype != GBS_F32) return fail(GBS_ERR_UNSUPPORTED, "batched launch supports GBS_F32 grids");
+  if (fp_mode != GBS_FP_EXACT && fp_mode != GBS_FP_FMA) return fail(GBS_ERR_INVALID, "bad fp_mode");
+  if (!out) return fail(GBS_ERR_INVALID, "out is NULL");
+  gbs_batch *h = nullptr;
+  gbs_status st = fp_mode == GBS_FP_FMA ? gbs_batch_build_1(grids, ngrids, &h) : gbs_batch_build_0(grids, ngrids, &h);
+  *out = h;
+  return st;
+}
+
+gbs_status gbs_batch_run(gbs_batch *plan, void *stream) {
+  auto *h = plan;
+  if (!h || !h->exec) return fail(GBS_ERR_INVALID, "batch plan is NULL");
+  cudaError_t e = cudaGraphLaunch(h->exec, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "batch: graph launch");
+  return GBS_OK;
+}
+
+gbs_status gbs_batch_info(const gbs_batch *plan, gbs_batch_stats *out) {
+  auto *h = plan;
+  if (!h || !out) return fail(GBS_ERR_INVALID, "NULL argument");
+  out->grids = h->ngrids;
+  out->items = h->nitems;
+  out->ctas = h->ctas;
+  out->cell_updates = h->cells;
+  out->plain_launches = h->launches_plain;
+  return GBS_OK;
+}
+
+void gbs_batch_destroy(gbs_batch *plan) {
+  auto *h = plan;
+  if (!h) return;
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  if (h->d_grids) cudaFree(h->d_grids);
+  if (h->d_items) cudaFree(h->d_items);
+  if (h->d_counters) cudaFree(h->d_counters);
+  delete h;
+}
+}  // extern "C"
+#endif

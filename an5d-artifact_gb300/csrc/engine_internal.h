@@ -48,5 +48,6 @@ gbs_status validate2d(const Layout &L, const Geometry2D &g);
 gbs_status error_word(int **out);
 gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_t stream, int *err);
 int max_bt(int sid, int dtype, int fma);
+bool div_proven_exact(double d);
 
 }  // namespace gbs

@@ -121,11 +121,12 @@ template <typename T, int V>
 __device__ __forceinline__ void ld_vec_global(T (&x)[V], const T *p) {
   Vec<T, V> t;
   if constexpr (sizeof(T) * V == 16) {
+    // cached in L2 only: a batched launch rewrites grids it reads
     if constexpr (std::is_same<T, float>::value) {
-      float4 f = __ldg(reinterpret_cast<const float4 *>(p));
+      float4 f = __ldcg(reinterpret_cast<const float4 *>(p));
       t.v[0] = f.x; t.v[1] = f.y; t.v[2] = f.z; t.v[3] = f.w;
     } else {
-      double2 f = __ldg(reinterpret_cast<const double2 *>(p));
+      double2 f = __ldcg(reinterpret_cast<const double2 *>(p));
       t.v[0] = f.x; t.v[1] = f.y;
     }
   } else {

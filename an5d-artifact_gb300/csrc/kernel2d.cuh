@@ -218,9 +218,16 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
   for (int e = 0; e < V; ++e) x[e] = y[e];
 }
 
-template <class ST, typename T, int B, bool FMA, int WPC, int NSTAGE>
-__global__ void __launch_bounds__(WPC * 32)
-    stencil2d_kernel(const __grid_constant__ Params2D<T, ST::kTerms> p) {
+// One work item of a warp: output columns [cs, ce) of strip `strip` and
+// output rows [i0, i1) of stream block `blk`, advanced by B levels from p.src
+// into p.dst. `ring`/`bars` are the warp's NSTAGE row buffers and their
+// mbarriers (initialised by the caller); `load_base` counts the copies this
+// warp has issued on them so far, so that items can follow each other on the
+// same barriers. Returns false when a bounded wait gave up (p.err is set and
+// the copies in flight have been drained).
+template <class ST, typename T, int B, bool FMA, int NSTAGE>
+__device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, int strip, int blk, T *ring,
+                                            uint64_t *bars, unsigned &load_base) {
   constexpr int V = 16 / sizeof(T);
   constexpr int R = ST::kRad;
   constexpr int W = 2 * R + 1;
@@ -228,14 +235,7 @@ __global__ void __launch_bounds__(WPC * 32)
   constexpr int NPH = UNR ? W : 1;
   constexpr int ROW = 32 * V;
   constexpr unsigned ROW_BYTES = ROW * sizeof(T);
-
-  extern __shared__ __align__(128) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
-  const long long gw = (long long)blockIdx.x * WPC + wid;
-  if (gw >= (long long)p.nstrips * p.nblocks) return;
-  const int strip = (int)(gw % p.nstrips);
-  const int blk = (int)(gw / p.nstrips);
 
   // ---- columns (column space c; offset space c + shift) ----
   const int cs = R + strip * p.wout;
@@ -254,22 +254,17 @@ __global__ void __launch_bounds__(WPC * 32)
   const int plast = i1 - 1 + B * R;        // last pipeline step
   const int nload = pend - pstart;
 
-  T *ring = reinterpret_cast<T *>(smem_raw) + (size_t)wid * NSTAGE * ROW;
-  uint64_t *bars =
-      reinterpret_cast<uint64_t *>(smem_raw + (size_t)WPC * NSTAGE * ROW_BYTES) + wid * NSTAGE;
   const T *src_win = p.src + ws;
   const T *src_lane = src_win + lane * V;
   T *dst_lane = p.dst + ws + lane * V;
+  const unsigned base = load_base;
 
   if (lane == 0) {
-#pragma unroll
-    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
-    fence_mbar_init();
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 #pragma unroll 1
-    for (int s = 0; s < NSTAGE && s < nload; ++s) {
+    for (int n = 0; n < NSTAGE && n < nload; ++n) {
+      const unsigned s = (base + n) % NSTAGE;
       mbar_arrive_expect_tx(&bars[s], ROW_BYTES);
-      bulk_g2s(ring + s * ROW, src_win + (long long)(pstart + s) * p.pitch, ROW_BYTES, &bars[s]);
+      bulk_g2s(ring + s * ROW, src_win + (long long)(pstart + n) * p.pitch, ROW_BYTES, &bars[s]);
     }
   }
   __syncwarp();
@@ -293,9 +288,10 @@ __global__ void __launch_bounds__(WPC * 32)
     T x[V];
     if (!careful || pp < pend) {
       const int n = pp - pstart;
-      const int s = n % NSTAGE;
+      const unsigned gn = base + n;
+      const unsigned s = gn % NSTAGE;
       // every lane waits; the decision to give up is warp-uniform
-      const bool got = mbar_wait(&bars[s], (unsigned)(n / NSTAGE) & 1u, nullptr, 0);
+      const bool got = mbar_wait(&bars[s], (gn / NSTAGE) & 1u, nullptr, 0);
       if (!__all_sync(0xffffffffu, got)) {
         if (lane == 0) atomicOr(p.err, ERR_WAIT_TIMEOUT);
         ok = false;
@@ -355,13 +351,49 @@ __global__ void __launch_bounds__(WPC * 32)
     if (z < plast + 1) run(z, plast + 1, IC<1>());
   }
 
-  if (!ok && lane == 0) {
-    // Timed out: wait (bounded) for the copies still in flight into this
-    // warp's ring before the CTA may exit and release its shared memory.
-    const int issued = min(nload, consumed + NSTAGE);
-    for (int n = consumed; n < issued; ++n)
-      if (!mbar_wait(&bars[n % NSTAGE], (unsigned)(n / NSTAGE) & 1u, p.err, ERR_DRAIN_TIMEOUT)) break;
+  if (!ok) {
+    if (lane == 0) {
+      // Timed out: wait (bounded) for the copies still in flight into this
+      // warp's ring before the CTA may exit and release its shared memory.
+      const int issued = min(nload, consumed + NSTAGE);
+      for (int n = consumed; n < issued; ++n) {
+        const unsigned gn = base + n;
+        if (!mbar_wait(&bars[gn % NSTAGE], (gn / NSTAGE) & 1u, p.err, ERR_DRAIN_TIMEOUT)) break;
+      }
+    }
+    return false;
   }
+  load_base = base + nload;
+  return true;
+}
+
+// The warp's ring and barriers inside the CTA's dynamic shared memory.
+template <typename T, int WPC, int NSTAGE>
+__device__ __forceinline__ void warp_ring2d(unsigned char *smem_raw, T *&ring, uint64_t *&bars) {
+  constexpr int ROW = 32 * (16 / sizeof(T));
+  const int wid = threadIdx.x >> 5;
+  ring = reinterpret_cast<T *>(smem_raw) + (size_t)wid * NSTAGE * ROW;
+  bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)WPC * NSTAGE * ROW * sizeof(T)) + wid * NSTAGE;
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncwarp();
+}
+
+template <class ST, typename T, int B, bool FMA, int WPC, int NSTAGE>
+__global__ void __launch_bounds__(WPC * 32)
+    stencil2d_kernel(const __grid_constant__ Params2D<T, ST::kTerms> p) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const long long gw = (long long)blockIdx.x * WPC + (threadIdx.x >> 5);
+  if (gw >= (long long)p.nstrips * p.nblocks) return;
+  T *ring;
+  uint64_t *bars;
+  warp_ring2d<T, WPC, NSTAGE>(smem_raw, ring, bars);
+  unsigned load_base = 0;
+  warp_item2d<ST, T, B, FMA, NSTAGE>(p, (int)(gw % p.nstrips), (int)(gw / p.nstrips), ring, bars, load_base);
 }
 
 constexpr int kWpc2D = 4, kStages2D = 8;

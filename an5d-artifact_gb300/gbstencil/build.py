@@ -51,8 +51,10 @@ def units():
                 out.append((name, CSRC / "inst.cu",
                             [f"-DGBS_SID={sid}", f"-DGBS_T={T}", f"-DGBS_FMA={fma}",
                              f"-DGBS_PICK=picks_{sid}_{t}_{m}"]))
+    for m in (0, 1):  # the batched kernel, exact and FMA mode
+        out.append((f"batch_{m}", CSRC / "batch.cu", [f"-DGBS_FMA={m}"]))
     for src in sorted(CSRC.glob("*.cu")):
-        if src.name != "inst.cu":
+        if src.name not in ("inst.cu", "batch.cu"):
             out.append((src.stem, src, []))
     return out
 

@@ -51,6 +51,16 @@ class PlanInfo(ctypes.Structure):
                 ("redundancy", ctypes.c_double)]
 
 
+class BatchGrid(ctypes.Structure):
+    _fields_ = [("stencil", ctypes.c_int), ("n", ctypes.c_int * 2), ("timestep", ctypes.c_int),
+                ("dev_A", ctypes.c_void_p), ("coef", ctypes.c_void_p), ("divisor", ctypes.c_double)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("grids", ctypes.c_int), ("items", ctypes.c_int), ("ctas", ctypes.c_int),
+                ("plain_launches", ctypes.c_int), ("cell_updates", ctypes.c_longlong)]
+
+
 _lib = None
 
 # every entry point the header declares: (name, restype, argtypes)
@@ -66,6 +76,11 @@ SIGNATURES = [
     ("gbs_upload", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_download", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_sync", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbs_batch_plan", ctypes.c_int, [ctypes.POINTER(BatchGrid), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_void_p)]),
+    ("gbs_batch_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("gbs_batch_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchStats)]),
+    ("gbs_batch_destroy", None, [ctypes.c_void_p]),
     ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gbs_check_division", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_longlong,
                                           ctypes.POINTER(ctypes.c_longlong)]),
@@ -170,6 +185,47 @@ def download(desc: Desc, dev_ptr: int, host_ptr: int, stream: int = 0):
 
 def sync(stream: int = 0):
     check(lib().gbs_sync(ctypes.c_void_p(stream)))
+
+
+class Batch:
+    """A planned batched launch (gbs_batch_plan) over device grids."""
+
+    def __init__(self, grids, fp_mode="fma"):
+        """grids: list of (DeviceGrid-like with .name, .n, .buf, timestep, coef or None)."""
+        arr = (BatchGrid * len(grids))()
+        self._keep = []
+        for i, (g, T, coef) in enumerate(grids):
+            arr[i].stencil = stencil_id(g.name)
+            arr[i].n[0], arr[i].n[1] = int(g.n[0]), int(g.n[1])
+            arr[i].timestep = int(T)
+            arr[i].dev_A = g.buf.data_ptr()
+            if coef is not None:
+                c = np.ascontiguousarray(coef, dtype=np.float32)
+                self._keep.append(c)
+                arr[i].coef = c.ctypes.data
+            arr[i].divisor = 0.0
+        h = ctypes.c_void_p()
+        check(lib().gbs_batch_plan(arr, len(grids), GBS_F32, FP_MODES[fp_mode], ctypes.byref(h)))
+        self.handle = h
+
+    def run(self, stream: int = 0):
+        check(lib().gbs_batch_run(self.handle, ctypes.c_void_p(stream)))
+
+    def stats(self) -> BatchStats:
+        st = BatchStats()
+        check(lib().gbs_batch_info(self.handle, ctypes.byref(st)))
+        return st
+
+    def close(self):
+        if self.handle:
+            lib().gbs_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def measure_fp_peak(dtype) -> float:

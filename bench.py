@@ -8,6 +8,11 @@ A step is one full time loop (T timesteps) over each grid of the workload:
 * suite3d (default): star3d2r and box3d1r, fp32 and fp64, 512^3 interior,
   T=1000, each at the fused degree the planner picks.
 * star2d1r: star2d1r fp32, 4096^2 interior, T=100.
+* batched: 512 independent fp32 2-D grids, sides log-uniform in [128, 4096]
+  per axis, stencil uniform over star2d1r-4r, box2d1r-4r, j2d5pt, j2d9pt,
+  T uniform in [16, 512], normalised random coefficients per grid, all
+  advanced by ONE persistent CUDA-graph launch; the line also reports the
+  same work done by per-grid plain launches, one grid after another.
 
 Inputs are synthetic: every cell (halo included) i.i.d. U[0,1) from a fixed
 seed, coefficients U[0,1) normalised to sum 1. ``value`` is GCells/s
@@ -46,6 +51,21 @@ WORKLOADS = {
                 ("box3d1r", np.float32, 512, 1000), ("box3d1r", np.float64, 512, 1000)],
     "star2d1r": [("star2d1r", np.float32, 4096, 100)],
 }
+
+
+BATCH_MIX = ["star2d1r", "star2d2r", "star2d3r", "star2d4r", "box2d1r", "box2d2r", "box2d3r", "box2d4r",
+             "j2d5pt", "j2d9pt"]
+
+
+def batched_specs(count=512, seed=20250101):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = [int(round(np.exp(rng.uniform(np.log(128), np.log(4096))))) for _ in range(2)]
+        name = BATCH_MIX[int(rng.integers(len(BATCH_MIX)))]
+        T = int(rng.integers(16, 513))
+        out.append((name, n, T))
+    return out
 
 
 def load_peaks():
@@ -297,13 +317,123 @@ def run_reference(args, rank, world):
     }
 
 
+def run_batched(args, rank, world):
+    import torch
+    from gbstencil import capi
+    from gbstencil.grid import DeviceGrid
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    specs = batched_specs()
+    if world > 1:  # weak scaling: each rank its own 512 grids
+        specs = batched_specs(seed=20250101 + rank)
+    grids, entries = [], []
+    for i, (name, n, T) in enumerate(specs):
+        g = DeviceGrid(name, np.float32, n, device=dev)
+        g.fill_uniform(seed=7 + i)
+        c = random_coefficients(name, np.float32, 3000 + i)
+        grids.append(g)
+        entries.append((g, T, c))
+    stream = torch.cuda.current_stream(dev)
+    batch = capi.Batch(entries, fp_mode=args.fp_mode)
+    st = batch.stats()
+    cells = st.cell_updates
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        batch.run(stream.cuda_stream)
+    capi.sync(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms = 0.0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0.record(stream)
+            batch.run(stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+    capi.sync(stream.cuda_stream)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = cells * world / (ms_step * 1e-3) / 1e9
+
+    # the same work as per-grid plain launches, one grid after another
+    def plain():
+        for g, T, c in entries:
+            g.run(T, args.fp_mode, 0, 0, coef=c)
+    plain()
+    capi.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+    flush.fill_(1.0)
+    e0.record(stream)
+    plain()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    capi.sync(stream.cuda_stream)
+    plain_ms = e0.elapsed_time(e1)
+    plain_launches = 0
+    for g, T, c in entries:
+        d, _ = g.desc(T, args.fp_mode, 0, 0, coef=c)
+        plain_launches += capi.plan(d).launches
+
+    # end to end: pinned host grids in, one batched replay, grids out
+    hosts = []
+    for g in grids:
+        h = torch.empty((2,) + tuple(g.dimsize), dtype=torch.float32).pin_memory()
+        h.copy_(torch.from_numpy(g.download()))
+        hosts.append(h)
+    def e2e_step():
+        for g, h in zip(grids, hosts):
+            g.upload(h.numpy(), stream=stream.cuda_stream)
+        batch.run(stream.cuda_stream)
+        for g, h in zip(grids, hosts):
+            g.download(h.numpy(), stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+    e2e_step()
+    t0 = time.perf_counter()
+    e2e_step()
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    capi.sync(stream.cuda_stream)
+    hbytes = sum(int(h.numel()) * 4 for h in hosts)
+    hbm, peak_kind = load_peaks()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: 512 seeded grids, U[0,1) cells, normalised U[0,1) coefficients",
+        "config": {"workload": "batched", "grids": len(specs), "cell_updates": cells,
+                   "sides": "log-uniform [128, 4096] per axis", "T": "uniform [16, 512]",
+                   "stencils": BATCH_MIX, "fp_mode": args.fp_mode, "items": st.items, "ctas": st.ctas,
+                   "l2": "flushed between timed steps (512 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "batched_vs_plain": {"plain_gcells_s": round(cells / (plain_ms * 1e-3) / 1e9, 3),
+                             "plain_ms": round(plain_ms, 3), "plain_launches": plain_launches,
+                             "batched_launches": 1, "ratio": round(plain_ms / ms_step, 3)},
+        "e2e": {"value": round(cells * world / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GCells/s",
+                "h2d_bytes_per_step": hbytes, "d2h_bytes_per_step": hbytes},
+        "roofline": {"bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+                     "traffic": None, "kernel": "batch2d_kernel",
+                     "note": "mixed stencils and degrees: see the per-stencil lines of the plain workloads"},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps,
+    }
+    batch.close()
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="suite3d", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="suite3d", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--fp-mode", default="fma", choices=["fma", "exact"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
@@ -317,9 +447,9 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    line = run_ours(args, rank, world)
+    line = run_batched(args, rank, world) if args.workload == "batched" else run_ours(args, rank, world)
     if rank == 0:
-        if not args.no_cpu:
+        if not args.no_cpu and args.workload != "batched":
             import pyoracle as po
             v, sample = cpu_sample(WORKLOADS[args.workload])
             line["cpu_baseline"] = {"value": round(v, 4), "unit": "GCells/s", "cores": po.max_threads(),

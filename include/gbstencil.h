@@ -132,6 +132,39 @@ gbs_status gbs_download(const gbs_desc *d, const void *dev_A, void *host_A, void
  * gave up) into GBS_ERR_TIMEOUT. */
 gbs_status gbs_sync(void *stream);
 
+/* ---- batched persistent launch ---------------------------------------- */
+/* Many independent 2-D grids (any mix of the 2-D stencils, sizes and step
+ * counts), advanced by ONE persistent kernel launch captured in a CUDA graph.
+ * No counterpart in the artifact, which runs one grid per process; this
+ * replaces a loop of per-grid kernel_stencil calls. */
+typedef struct gbs_batch_grid {
+  int stencil;        /* a 2-D stencil id */
+  int n[2];           /* interior extent per axis */
+  int timestep;       /* T >= 0 */
+  void *dev_A;        /* two-plane grid in the engine layout (gbs_get_layout of
+                         the same stencil, GBS_F32 and n), 128-byte aligned */
+  const void *coef;   /* NULL = the source literals, else nterms floats */
+  double divisor;     /* 0 = the source value */
+} gbs_batch_grid;
+
+typedef struct gbs_batch gbs_batch; /* opaque plan */
+
+typedef struct gbs_batch_stats {
+  int grids, items, ctas;
+  int plain_launches;      /* kernel launches the same work takes one grid at a time */
+  long long cell_updates;  /* sum of n[0]*n[1]*timestep */
+} gbs_batch_stats;
+
+/* Plans the batch: work items, per-grid dependency counters and the CUDA
+ * graph (counter reset + the persistent kernel). Allocates device memory
+ * owned by the plan. dtype must be GBS_F32. The grids' buffers must stay
+ * valid while the plan is used. */
+gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, gbs_batch **out);
+/* Replays the plan's graph on `stream` (asynchronous; see gbs_sync). */
+gbs_status gbs_batch_run(gbs_batch *plan, void *stream);
+gbs_status gbs_batch_info(const gbs_batch *plan, gbs_batch_stats *out);
+void gbs_batch_destroy(gbs_batch *plan);
+
 /* Measures the device's fused multiply-add throughput in GFLOP/s (2 flops per
  * FMA): the FP term of the temporally-blocked stencil roofline. */
 gbs_status gbs_measure_fp_peak(int dtype, double *gflops);
