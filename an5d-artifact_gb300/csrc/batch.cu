@@ -8,8 +8,9 @@
 // persistent warps take them in that order from an atomic counter. An item
 // of time block k of grid g starts once every item of g's earlier blocks has
 // finished (a per-grid completion counter reaching the item's `need`). The
-// order makes this deadlock-free: every item an item waits on was taken
-// earlier by a running warp that never waits on a later item. Waits are
+// order (by stencil, then time block) makes this deadlock-free: every item
+// an item waits on was taken earlier by a running warp that never waits on a
+// later item. Waits are
 // bounded (the error word is set and the warp stops).
 //
 // Memory ordering: a finishing item's lanes fence their stores, then lane 0
@@ -82,49 +83,70 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
+// bytes of the per-warp shared-memory slot that holds an item's parameters
+constexpr int kParamSlot = 512;
+static_assert(sizeof(Params2D<float, batchdetail::kMaxTerms>) <= kParamSlot, "parameter slot too small");
+
+// One (stencil, degree) variant per function, not inlined: each variant gets
+// its own register allocation (inlining all of them into the dispatcher
+// forces a local-memory frame onto every variant's loop) and the call costs
+// once per item. The parameters (with up to 81 coefficients) are staged in
+// shared memory: a per-thread copy would sit on the local-memory stack.
 template <class S, int B>
-__device__ __forceinline__ bool run_item(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
-                                         unsigned &load_base, int *err) {
-  Params2D<float, S::kTerms> p;
-  p.src = g.base + (long long)(it.k % 2) * g.plane;
-  p.dst = g.base + (long long)((it.k + 1) % 2) * g.plane;
-  p.err = err;
-  p.pitch = g.pitch;
-  p.d0 = g.d0;
-  p.d1 = g.d1;
-  p.shift = g.shift;
-  p.b = B;
-  p.wout = ((128 - 2 * B * S::kRad - 3) / 4) * 4;
-  p.nstrips = 0;
-  p.nblocks = g.nblocks;
-  p.sl = g.sl;
-#pragma unroll
-  for (int t = 0; t < S::kTerms; ++t) p.coef[t] = g.coef[t];
-  p.div = g.div;
-  p.rdiv = g.rdiv;
-  p.eps = g.eps;
-  p.divmode = g.divmode;
-  return warp_item2d<S, float, B, kFma, kStages>(p, it.strip, it.blk, ring, bars, load_base);
+__device__ __noinline__ bool run_item(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
+                                      unsigned &load_base, int *err, unsigned char *slot) {
+  auto &p = *reinterpret_cast<Params2D<float, S::kTerms> *>(slot);
+  const int lane = threadIdx.x & 31;
+  for (int t = lane; t < S::kTerms; t += 32) p.coef[t] = g.coef[t];
+  if (lane == 0) {
+    p.src = g.base + (long long)(it.k % 2) * g.plane;
+    p.dst = g.base + (long long)((it.k + 1) % 2) * g.plane;
+    p.err = err;
+    p.pitch = g.pitch;
+    p.d0 = g.d0;
+    p.d1 = g.d1;
+    p.shift = g.shift;
+    p.b = B;
+    p.wout = ((128 - 2 * B * S::kRad - 3) / 4) * 4;
+    p.nstrips = 0;
+    p.nblocks = g.nblocks;
+    p.sl = g.sl;
+    p.div = g.div;
+    p.rdiv = g.rdiv;
+    p.eps = g.eps;
+    p.divmode = g.divmode;
+  }
+  __syncwarp();
+  bool ok;
+  if constexpr (S::kTerms <= 25) {
+    // small parameter sets ride in registers for the whole item
+    const Params2D<float, S::kTerms> pl = p;
+    ok = warp_item2d<S, float, B, kFma, kStages>(pl, it.strip, it.blk, ring, bars, load_base);
+  } else {
+    ok = warp_item2d<S, float, B, kFma, kStages>(p, it.strip, it.blk, ring, bars, load_base);
+  }
+  __syncwarp();  // the slot is rewritten by the next item
+  return ok;
 }
 
 template <class S>
 __device__ __forceinline__ bool dispatch_b(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
-                                           unsigned &load_base, int *err) {
+                                           unsigned &load_base, int *err, unsigned char *slot) {
   constexpr int BS = batch_degree<S>();
-  if (it.b == BS) return run_item<S, BS>(g, it, ring, bars, load_base, err);
+  if (it.b == BS) return run_item<S, BS>(g, it, ring, bars, load_base, err, slot);
   if constexpr (BS != 1) {
-    if (it.b == 1) return run_item<S, 1>(g, it, ring, bars, load_base, err);
+    if (it.b == 1) return run_item<S, 1>(g, it, ring, bars, load_base, err, slot);
   }
   return false;
 }
 
-__device__ bool dispatch(const GridDev &g, const Item &it, float *ring, uint64_t *bars, unsigned &load_base,
-                         int *err) {
+__device__ __forceinline__ bool dispatch(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
+                                         unsigned &load_base, int *err, unsigned char *slot) {
   switch (g.sid) {
 #define GBS_CASE(id, S)                                                  \
   case id:                                                               \
     if constexpr (S::kDim == 2)                                          \
-      return dispatch_b<S>(g, it, ring, bars, load_base, err);           \
+      return dispatch_b<S>(g, it, ring, bars, load_base, err, slot);     \
     else                                                                 \
       return false;
     GBS_FOR_EACH_STENCIL(GBS_CASE)
@@ -134,12 +156,14 @@ __device__ bool dispatch(const GridDev &g, const Item &it, float *ring, uint64_t
   }
 }
 
-__global__ void __launch_bounds__(kWpc * 32, 4) batch2d_kernel(const __grid_constant__ Args a) {
+__global__ void __launch_bounds__(kWpc * 32, 3) batch2d_kernel(const __grid_constant__ Args a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float *ring;
   uint64_t *bars;
   warp_ring2d<float, kWpc, kStages>(smem_raw, ring, bars);
   const int lane = threadIdx.x & 31;
+  unsigned char *slot = smem_raw + (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t)) +
+                        (size_t)(threadIdx.x >> 5) * kParamSlot;
   unsigned load_base = 0;
   while (true) {
     unsigned idx = 0;
@@ -165,7 +189,7 @@ __global__ void __launch_bounds__(kWpc * 32, 4) batch2d_kernel(const __grid_cons
     }
     if (!__all_sync(0xffffffffu, ok)) break;
     __syncwarp();
-    if (!dispatch(a.grids[it.grid], it, ring, bars, load_base, a.err)) {
+    if (!dispatch(a.grids[it.grid], it, ring, bars, load_base, a.err, slot)) {
       if (lane == 0) atomicOr(a.err, ERR_WAIT_TIMEOUT);
       break;
     }
@@ -259,8 +283,9 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
     x.shift = (int)L.shift;
     x.sid = bg.stencil;
     const int ni = L.dims[0] - 2 * s->rad;
-    // stream blocks of about 128 rows keep items short for load balance
-    x.sl = std::min(ni, std::max(32, (ni + 7) / 8 > 128 ? 128 : (ni + 7) / 8 < 32 ? 32 : (ni + 7) / 8));
+    // stream blocks of up to 256 rows: long enough to amortise an item's
+    // start (dependency check, first copies), short enough to balance
+    x.sl = std::min(ni, 256);
     x.nblocks = (ni + x.sl - 1) / x.sl;
     const double div = bg.divisor != 0.0 ? bg.divisor : (double)s->divisor;
     const bool fold = kFma && s->divisor && div != 0.0;
@@ -283,14 +308,18 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
       if (st != GBS_OK) return st;
     }
   }
-  // items ordered by time block, grids interleaved within a block
+  // Items ordered by stencil, then time block, then grid: warps that run at
+  // the same time execute the same kernel variant (one instruction-cache
+  // working set), and every grid's blocks stay in order, so each item's
+  // dependencies come earlier in the list.
   std::vector<Item> items;
   std::vector<int> done_before(ngrids, 0);
   size_t kmax = 0;
   for (auto &b : blocks) kmax = std::max(kmax, b.size());
+  for (int sid = 0; sid < GBS_NUM_STENCILS; ++sid)
   for (size_t k = 0; k < kmax; ++k) {
     for (int g = 0; g < ngrids; ++g) {
-      if (k >= blocks[g].size()) continue;
+      if (grids[g].stencil != sid || k >= blocks[g].size()) continue;
       const int b = blocks[g][k];
       const gbs_stencil_def_t *s = stencil_def(grids[g].stencil);
       const int wout = ((128 - 2 * b * s->rad - 3) / 4) * 4;
@@ -322,7 +351,7 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
     gbs_batch_destroy(h);
     return st;
   }
-  h->smem = (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t));
+  h->smem = (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t)) + (size_t)kWpc * kParamSlot;
   int per_sm = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -142,6 +142,16 @@ __device__ __forceinline__ void st_vec(T *p, const T (&x)[V]) {
   for (int e = 0; e < V; ++e) t.v[e] = x[e];
   *reinterpret_cast<Vec<T, V> *>(p) = t;
 }
+// 16-byte store to global memory, marked as such so that the compiler knows
+// it cannot alias shared memory.
+template <typename T, int V>
+__device__ __forceinline__ void st_vec_global(T *p, const T (&x)[V]) {
+  static_assert(sizeof(T) * V == 16, "16-byte vectors only");
+  if constexpr (std::is_same<T, float>::value) __stcg(reinterpret_cast<float4 *>(p), make_float4(x[0], x[1], x[2], x[3]));
+  else __stcg(reinterpret_cast<double2 *>(p), make_double2(x[0], x[1]));
+}
+template <typename T>
+__device__ __forceinline__ void st_global(T *p, T v) { __stcg(p, v); }
 
 // ---- lane shuffles -----------------------------------------------------------
 template <typename T>

@@ -136,21 +136,20 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
           y[e] = gradient_update<T, ST::kTerms>(win[cslot][e], nb, p.eps, p.coef[0]);
         });
       } else {
-        T ext[W][V + 2 * R];
-        static_for<W>([&](auto DI) {
-          constexpr int di = decltype(DI)::value - R;
-          if constexpr (Tap2<ST, V>::row_has_dj(di))
-            extend_row<ST, V, di>(ext[di + R], win[wslot<UNR, W>(PH, R + di)]);
-        });
+        // the direct form serves stencils whose off-centre rows are read at
+        // the centre column only (stars, star2d4r): one extended row
+        T ext[V + 2 * R];
+        extend_row<ST, V, 0>(ext, win[cslot]);
         static_for<ST::kTerms>([&](auto TI) {
           constexpr int t = decltype(TI)::value;
           constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+          static_assert(di == 0 || dj == 0, "direct 2-D form expects off-centre rows at dj == 0");
           constexpr int slot = wslot<UNR, W>(PH, R + di);
           static_for<V>([&](auto EI) {
             constexpr int e = decltype(EI)::value;
             T a;
             if constexpr (dj == 0) a = win[slot][e];
-            else a = ext[di + R][R + e + dj];
+            else a = ext[R + e + dj];
             if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
             else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
           });
@@ -257,6 +256,7 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
   const T *src_win = p.src + ws;
   const T *src_lane = src_win + lane * V;
   T *dst_lane = p.dst + ws + lane * V;
+  const long long pitch = p.pitch;
   const unsigned base = load_base;
 
   if (lane == 0) {
@@ -302,7 +302,7 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
       __syncwarp();
       if (lane == 0 && n + NSTAGE < nload) {
         mbar_arrive_expect_tx(&bars[s], ROW_BYTES);
-        bulk_g2s(ring + s * ROW, src_win + (long long)(pp + NSTAGE) * p.pitch, ROW_BYTES, &bars[s]);
+        bulk_g2s(ring + s * ROW, src_win + (long long)(pp + NSTAGE) * pitch, ROW_BYTES, &bars[s]);
       }
     } else {
 #pragma unroll
@@ -314,13 +314,13 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
     });
     const int q = pp - B * R;
     if (q >= i0 && q < i1) {
-      T *d = dst_lane + (long long)q * p.pitch;
+      T *d = dst_lane + (long long)q * pitch;
       if (store_all) {
-        st_vec<T, V>(d, x);
+        st_vec_global<T, V>(d, x);
       } else {
 #pragma unroll
         for (int e = 0; e < V; ++e)
-          if (col0 + e >= cs && col0 + e < ce) d[e] = x[e];
+          if (col0 + e >= cs && col0 + e < ce) st_global(d + e, x[e]);
       }
     }
   };

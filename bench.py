@@ -57,13 +57,13 @@ BATCH_MIX = ["star2d1r", "star2d2r", "star2d3r", "star2d4r", "box2d1r", "box2d2r
              "j2d5pt", "j2d9pt"]
 
 
-def batched_specs(count=512, seed=20250101):
+def batched_specs(count=512, seed=20250101, tmax=512):
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         n = [int(round(np.exp(rng.uniform(np.log(128), np.log(4096))))) for _ in range(2)]
         name = BATCH_MIX[int(rng.integers(len(BATCH_MIX)))]
-        T = int(rng.integers(16, 513))
+        T = int(rng.integers(16, tmax + 1))
         out.append((name, n, T))
     return out
 
@@ -324,9 +324,9 @@ def run_batched(args, rank, world):
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
-    specs = batched_specs()
-    if world > 1:  # weak scaling: each rank its own 512 grids
-        specs = batched_specs(seed=20250101 + rank)
+    specs = batched_specs(args.batch_grids, tmax=args.batch_tmax)
+    if world > 1:  # weak scaling: each rank its own grids
+        specs = batched_specs(args.batch_grids, seed=20250101 + rank, tmax=args.batch_tmax)
     grids, entries = [], []
     for i, (name, n, T) in enumerate(specs):
         g = DeviceGrid(name, np.float32, n, device=dev)
@@ -436,6 +436,8 @@ def main():
     ap.add_argument("--workload", default="suite3d", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--fp-mode", default="fma", choices=["fma", "exact"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
+    ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
