@@ -8,10 +8,9 @@
 // persistent warps take them in that order from an atomic counter. An item
 // of time block k of grid g starts once every item of g's earlier blocks has
 // finished (a per-grid completion counter reaching the item's `need`). The
-// order (by stencil, then time block) makes this deadlock-free: every item
-// an item waits on was taken earlier by a running warp that never waits on a
-// later item. Waits are
-// bounded (the error word is set and the warp stops).
+// order (by time block) makes this deadlock-free: every item an item waits
+// on was taken earlier by a running warp that never waits on a later item.
+// Waits are bounded (the error word is set and the warp stops).
 //
 // Memory ordering: a finishing item's lanes fence their stores, then lane 0
 // increments the grid's counter; a starting item's lane 0 reads the counter
@@ -283,9 +282,10 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
     x.shift = (int)L.shift;
     x.sid = bg.stencil;
     const int ni = L.dims[0] - 2 * s->rad;
-    // stream blocks of up to 256 rows: long enough to amortise an item's
-    // start (dependency check, first copies), short enough to balance
-    x.sl = std::min(ni, 256);
+    // stream blocks of up to 128 rows: long enough to amortise an item's
+    // start (dependency check, first copies), short enough that a time
+    // block's items finish together (a grid's blocks run one after another)
+    x.sl = std::min(ni, 128);
     x.nblocks = (ni + x.sl - 1) / x.sl;
     const double div = bg.divisor != 0.0 ? bg.divisor : (double)s->divisor;
     const bool fold = kFma && s->divisor && div != 0.0;
@@ -308,16 +308,18 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
       if (st != GBS_OK) return st;
     }
   }
-  // Items ordered by stencil, then time block, then grid: warps that run at
-  // the same time execute the same kernel variant (one instruction-cache
-  // working set), and every grid's blocks stay in order, so each item's
-  // dependencies come earlier in the list.
+  // Items ordered by time block, then stencil, then grid: every grid's
+  // blocks stay in order (each item's dependencies come earlier in the
+  // list), all grids advance together (the critical path is the longest
+  // grid's chain of blocks, not a sum over groups), and warps taking
+  // neighbouring items run the same kernel variant (one instruction-cache
+  // working set).
   std::vector<Item> items;
   std::vector<int> done_before(ngrids, 0);
   size_t kmax = 0;
   for (auto &b : blocks) kmax = std::max(kmax, b.size());
-  for (int sid = 0; sid < GBS_NUM_STENCILS; ++sid)
-  for (size_t k = 0; k < kmax; ++k) {
+  for (size_t k = 0; k < kmax; ++k)
+  for (int sid = 0; sid < GBS_NUM_STENCILS; ++sid) {
     for (int g = 0; g < ngrids; ++g) {
       if (grids[g].stencil != sid || k >= blocks[g].size()) continue;
       const int b = blocks[g][k];

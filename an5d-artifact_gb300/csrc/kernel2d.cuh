@@ -103,9 +103,30 @@ __device__ __forceinline__ void extend_row(T (&ext)[V + 2 * ST::kRad], const T (
 // One fused time level: the level-(l) row x arrives, the level-(l+1) row q
 // leaves in x. CAREFUL handles halo rows and columns (grid edges);
 // otherwise the caller guarantees that every row and column is interior.
-template <class ST, typename T, bool FMA, bool UNR, bool CAREFUL, int PH, int V>
+// Level-0 rows a warp's ring keeps after they arrive: the assoc form carries
+// halo cells of row q (up to b*r rows back) from the ring; the direct form
+// carries them from its register window.
+template <class ST, int B> constexpr int ring_keep2d() { return ST::kAssoc ? B * ST::kRad : 0; }
+
+// Where an assoc-form level finds the fixed halo values of row q: the warp's
+// ring, which still holds level-0 row q (load index q - pstart). Reading
+// them there costs a shared-memory load instead of a memory round trip in
+// every step of a warp at the grid's edge.
+template <typename T, int NSTAGE> struct CarryRing {
+  const T *ring;        // the warp's ring + lane * V
+  unsigned base;        // the item's first load index on the ring
+  int pstart;           // row of load index 0
+  int nrows;            // rows loaded by the item
+  __device__ __forceinline__ const T *row(int q) const {
+    const int n = q - pstart;
+    return (n >= 0 && n < nrows) ? ring + (size_t)((base + (unsigned)n) % NSTAGE) * (32 * (16 / sizeof(T)))
+                                 : nullptr;
+  }
+};
+
+template <class ST, typename T, bool FMA, bool UNR, bool CAREFUL, int PH, int V, int NSTAGE>
 __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V], int q, bool edge,
-                                        int col0, const T *src_row_base,
+                                        int col0, const CarryRing<T, NSTAGE> &carry,
                                         const Params2D<T, ST::kTerms> &p) {
   constexpr int R = ST::kRad;
   constexpr int W = 2 * R + 1;
@@ -196,14 +217,15 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
       for (int e = 0; e < V; ++e) y[e] = apply_div(y[e], p);
     }
     if constexpr (CAREFUL) {
-      if (halo_row) {
-        if (q >= 0 && q < p.d0) ld_vec_global<T, V>(y, src_row_base + (long long)q * p.pitch);
-      } else if (edge) {
-        T c[V];
-        ld_vec_global<T, V>(c, src_row_base + (long long)q * p.pitch);
+      if (halo_row || edge) {
+        const T *c = (q >= 0 && q < p.d0) ? carry.row(q) : nullptr;
+        if (c) {
+          T cv[V];
+          ld_vec<T, V>(cv, c);
 #pragma unroll
-        for (int e = 0; e < V; ++e)
-          if (col0 + e < R || col0 + e >= p.d1 - R) y[e] = c[e];
+          for (int e = 0; e < V; ++e)
+            if (halo_row || col0 + e < R || col0 + e >= p.d1 - R) y[e] = cv[e];
+        }
       }
     }
   }
@@ -254,10 +276,12 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
   const int nload = pend - pstart;
 
   const T *src_win = p.src + ws;
-  const T *src_lane = src_win + lane * V;
   T *dst_lane = p.dst + ws + lane * V;
   const long long pitch = p.pitch;
   const unsigned base = load_base;
+  constexpr int KEEP = ring_keep2d<ST, B>();
+  static_assert(KEEP + 2 <= NSTAGE, "the ring must keep b*r rows and still prefetch");
+  const CarryRing<T, NSTAGE> carry{ring + lane * V, base, pstart, nload};
 
   if (lane == 0) {
 #pragma unroll 1
@@ -299,18 +323,13 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
       }
       ld_vec<T, V>(x, ring + s * ROW + lane * V);
       consumed = n + 1;
-      __syncwarp();
-      if (lane == 0 && n + NSTAGE < nload) {
-        mbar_arrive_expect_tx(&bars[s], ROW_BYTES);
-        bulk_g2s(ring + s * ROW, src_win + (long long)(pp + NSTAGE) * pitch, ROW_BYTES, &bars[s]);
-      }
     } else {
 #pragma unroll
       for (int e = 0; e < V; ++e) x[e] = T(0);
     }
     static_for<B>([&](auto LI) {
       constexpr int l = decltype(LI)::value;
-      level2d<ST, T, FMA, UNR, careful, ph, V>(win[l], x, pp - (l + 1) * R, edge, col0, src_lane, p);
+      level2d<ST, T, FMA, UNR, careful, ph, V, NSTAGE>(win[l], x, pp - (l + 1) * R, edge, col0, carry, p);
     });
     const int q = pp - B * R;
     if (q >= i0 && q < i1) {
@@ -321,6 +340,16 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
 #pragma unroll
         for (int e = 0; e < V; ++e)
           if (col0 + e >= cs && col0 + e < ce) st_global(d + e, x[e]);
+      }
+    }
+    // the row KEEP steps back is no longer needed: refill its stage
+    const int nf = pp - pstart - KEEP;
+    if (nf >= 0 && nf + NSTAGE < nload) {
+      __syncwarp();
+      if (lane == 0) {
+        const unsigned sf = (base + nf) % NSTAGE;
+        mbar_arrive_expect_tx(&bars[sf], ROW_BYTES);
+        bulk_g2s(ring + sf * ROW, src_win + (long long)(pstart + nf + NSTAGE) * pitch, ROW_BYTES, &bars[sf]);
       }
     }
   };
@@ -355,7 +384,7 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
     if (lane == 0) {
       // Timed out: wait (bounded) for the copies still in flight into this
       // warp's ring before the CTA may exit and release its shared memory.
-      const int issued = min(nload, consumed + NSTAGE);
+      const int issued = min(nload, max(NSTAGE, consumed + NSTAGE - KEEP));
       for (int n = consumed; n < issued; ++n) {
         const unsigned gn = base + n;
         if (!mbar_wait(&bars[gn % NSTAGE], (gn / NSTAGE) & 1u, p.err, ERR_DRAIN_TIMEOUT)) break;
@@ -396,7 +425,7 @@ __global__ void __launch_bounds__(WPC * 32)
   warp_item2d<ST, T, B, FMA, NSTAGE>(p, (int)(gw % p.nstrips), (int)(gw / p.nstrips), ring, bars, load_base);
 }
 
-constexpr int kWpc2D = 4, kStages2D = 8;
+constexpr int kWpc2D = 4, kStages2D = 16;
 
 template <class ST, typename T, int B, bool FMA>
 int occupancy2d() {
