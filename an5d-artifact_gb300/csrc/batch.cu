@@ -198,6 +198,24 @@ __global__ void __launch_bounds__(kWpc * 32, 3) batch2d_kernel(const __grid_cons
   }
 }
 
+// One time block of every grid: warp w runs item first + w. Kernel
+// boundaries order the blocks, so nothing here waits.
+__global__ void __launch_bounds__(kWpc * 32, 3) batch_layer_kernel(const __grid_constant__ Args a, int first,
+                                                                   int count) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const long long gw = (long long)blockIdx.x * kWpc + (threadIdx.x >> 5);
+  if (gw >= count) return;
+  float *ring;
+  uint64_t *bars;
+  warp_ring2d<float, kWpc, kStages>(smem_raw, ring, bars);
+  unsigned char *slot = smem_raw + (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t)) +
+                        (size_t)(threadIdx.x >> 5) * kParamSlot;
+  unsigned load_base = 0;
+  const Item it = a.items[first + gw];
+  if (!dispatch(a.grids[it.grid], it, ring, bars, load_base, a.err, slot) && (threadIdx.x & 31) == 0)
+    atomicOr(a.err, ERR_WAIT_TIMEOUT);
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -244,13 +262,15 @@ struct gbs_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int launches_plain = 0;          // what per-grid plain launches would need
+  int mode = 0, kernels = 0;
 };
 
 #define GBS_BATCH_FN(name) GBS_BATCH_FN2(name, GBS_FMA)
 #define GBS_BATCH_FN2(name, m) GBS_BATCH_FN3(name, m)
 #define GBS_BATCH_FN3(name, m) name##_##m
 
-extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grids, int ngrids, gbs_batch **out) {
+extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grids, int ngrids, int mode,
+                                                       gbs_batch **out) {
   if (!grids || ngrids <= 0 || !out) return fail(GBS_ERR_INVALID, "batch: no grids");
   std::vector<GridDev> gd(ngrids);
   std::vector<std::vector<int>> blocks(ngrids);
@@ -318,8 +338,10 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
   std::vector<int> done_before(ngrids, 0);
   size_t kmax = 0;
   for (auto &b : blocks) kmax = std::max(kmax, b.size());
+  std::vector<int> layer_start;
   for (size_t k = 0; k < kmax; ++k)
   for (int sid = 0; sid < GBS_NUM_STENCILS; ++sid) {
+    if (sid == 0) layer_start.push_back((int)items.size());
     for (int g = 0; g < ngrids; ++g) {
       if (grids[g].stencil != sid || k >= blocks[g].size()) continue;
       const int b = blocks[g][k];
@@ -377,10 +399,22 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
     gbs_batch_destroy(h);
     return cuda_fail(e, "batch: stream");
   }
+  layer_start.push_back((int)items.size());
+  h->mode = mode;
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned) * (ngrids + 1), cs);
-    batch2d_kernel<<<h->ctas, kWpc * 32, h->smem, cs>>>(a);
+    if (mode == GBS_BATCH_LAYERED) {
+      for (size_t k = 0; k + 1 < layer_start.size(); ++k) {
+        const int first = layer_start[k], count = layer_start[k + 1] - first;
+        if (count <= 0) continue;
+        batch_layer_kernel<<<(count + kWpc - 1) / kWpc, kWpc * 32, h->smem, cs>>>(a, first, count);
+        ++h->kernels;
+      }
+    } else {
+      cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned) * (ngrids + 1), cs);
+      batch2d_kernel<<<h->ctas, kWpc * 32, h->smem, cs>>>(a);
+      h->kernels = 1;
+    }
     e = cudaStreamEndCapture(cs, &h->graph);
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&h->exec, h->graph, 0);
@@ -395,15 +429,18 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
 
 #if GBS_FMA
 // The C ABI entry points live in the FMA unit; they dispatch on fp_mode.
-extern "C++" gbs_status gbs_batch_build_0(const gbs_batch_grid *, int, gbs_batch **);
+extern "C++" gbs_status gbs_batch_build_0(const gbs_batch_grid *, int, int, gbs_batch **);
 
 extern "C" {
-gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, gbs_batch **out) {
+gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, int mode,
+                          gbs_batch **out) {
+  if (mode != GBS_BATCH_PERSISTENT && mode != GBS_BATCH_LAYERED) return fail(GBS_ERR_INVALID, "bad batch mode");
   if (dtype != GBS_F32) return fail(GBS_ERR_UNSUPPORTED, "batched launch supports GBS_F32 grids");
   if (fp_mode != GBS_FP_EXACT && fp_mode != GBS_FP_FMA) return fail(GBS_ERR_INVALID, "bad fp_mode");
   if (!out) return fail(GBS_ERR_INVALID, "out is NULL");
   gbs_batch *h = nullptr;
-  gbs_status st = fp_mode == GBS_FP_FMA ? gbs_batch_build_1(grids, ngrids, &h) : gbs_batch_build_0(grids, ngrids, &h);
+  gbs_status st = fp_mode == GBS_FP_FMA ? gbs_batch_build_1(grids, ngrids, mode, &h)
+                                        : gbs_batch_build_0(grids, ngrids, mode, &h);
   *out = h;
   return st;
 }
@@ -424,6 +461,8 @@ gbs_status gbs_batch_info(const gbs_batch *plan, gbs_batch_stats *out) {
   out->ctas = h->ctas;
   out->cell_updates = h->cells;
   out->plain_launches = h->launches_plain;
+  out->kernels = h->kernels;
+  out->mode = h->mode;
   return GBS_OK;
 }
 

@@ -58,7 +58,8 @@ class BatchGrid(ctypes.Structure):
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("grids", ctypes.c_int), ("items", ctypes.c_int), ("ctas", ctypes.c_int),
-                ("plain_launches", ctypes.c_int), ("cell_updates", ctypes.c_longlong)]
+                ("plain_launches", ctypes.c_int), ("cell_updates", ctypes.c_longlong),
+                ("kernels", ctypes.c_int), ("mode", ctypes.c_int)]
 
 
 _lib = None
@@ -77,7 +78,7 @@ SIGNATURES = [
     ("gbs_download", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_sync", ctypes.c_int, [ctypes.c_void_p]),
     ("gbs_batch_plan", ctypes.c_int, [ctypes.POINTER(BatchGrid), ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                      ctypes.POINTER(ctypes.c_void_p)]),
+                                      ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     ("gbs_batch_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_batch_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchStats)]),
     ("gbs_batch_destroy", None, [ctypes.c_void_p]),
@@ -190,7 +191,9 @@ def sync(stream: int = 0):
 class Batch:
     """A planned batched launch (gbs_batch_plan) over device grids."""
 
-    def __init__(self, grids, fp_mode="fma"):
+    MODES = {"persistent": 0, "layered": 1}
+
+    def __init__(self, grids, fp_mode="fma", mode="persistent"):
         """grids: list of (DeviceGrid-like with .name, .n, .buf, timestep, coef or None)."""
         arr = (BatchGrid * len(grids))()
         self._keep = []
@@ -205,7 +208,8 @@ class Batch:
                 arr[i].coef = c.ctypes.data
             arr[i].divisor = 0.0
         h = ctypes.c_void_p()
-        check(lib().gbs_batch_plan(arr, len(grids), GBS_F32, FP_MODES[fp_mode], ctypes.byref(h)))
+        check(lib().gbs_batch_plan(arr, len(grids), GBS_F32, FP_MODES[fp_mode], self.MODES[mode],
+                                   ctypes.byref(h)))
         self.handle = h
 
     def run(self, stream: int = 0):

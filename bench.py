@@ -335,7 +335,7 @@ def run_batched(args, rank, world):
         grids.append(g)
         entries.append((g, T, c))
     stream = torch.cuda.current_stream(dev)
-    batch = capi.Batch(entries, fp_mode=args.fp_mode)
+    batch = capi.Batch(entries, fp_mode=args.fp_mode, mode=args.batch_mode)
     st = batch.stats()
     cells = st.cell_updates
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -410,6 +410,7 @@ def run_batched(args, rank, world):
         "config": {"workload": "batched", "grids": len(specs), "cell_updates": cells,
                    "sides": "log-uniform [128, 4096] per axis", "T": "uniform [16, 512]",
                    "stencils": BATCH_MIX, "fp_mode": args.fp_mode, "items": st.items, "ctas": st.ctas,
+                   "batch_mode": args.batch_mode, "graph_kernels": st.kernels,
                    "l2": "flushed between timed steps (512 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "batched_vs_plain": {"plain_gcells_s": round(cells / (plain_ms * 1e-3) / 1e9, 3),
@@ -438,6 +439,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
+    ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "layered"],
+                    help="batched workload: scheduling of the work items")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

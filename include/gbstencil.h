@@ -153,13 +153,26 @@ typedef struct gbs_batch_stats {
   int grids, items, ctas;
   int plain_launches;      /* kernel launches the same work takes one grid at a time */
   long long cell_updates;  /* sum of n[0]*n[1]*timestep */
+  int kernels;             /* kernel nodes in the plan's graph */
+  int mode;                /* GBS_BATCH_PERSISTENT | GBS_BATCH_LAYERED */
 } gbs_batch_stats;
+
+/* How a batch plan schedules its work items (grid, time block, strip,
+ * stream block):
+ * GBS_BATCH_PERSISTENT: one persistent kernel; warps take items in time-block
+ *   order from an atomic counter and wait (bounded) on per-grid completion
+ *   counters for the grid's previous time block.
+ * GBS_BATCH_LAYERED: one kernel node per time block in the graph, each over
+ *   every grid's items of that block; kernel boundaries order the blocks, so
+ *   nothing waits on the device. */
+enum { GBS_BATCH_PERSISTENT = 0, GBS_BATCH_LAYERED = 1 };
 
 /* Plans the batch: work items, per-grid dependency counters and the CUDA
  * graph (counter reset + the persistent kernel). Allocates device memory
  * owned by the plan. dtype must be GBS_F32. The grids' buffers must stay
  * valid while the plan is used. */
-gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, gbs_batch **out);
+gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, int mode,
+                          gbs_batch **out);
 /* Replays the plan's graph on `stream` (asynchronous; see gbs_sync). */
 gbs_status gbs_batch_run(gbs_batch *plan, void *stream);
 gbs_status gbs_batch_info(const gbs_batch *plan, gbs_batch_stats *out);

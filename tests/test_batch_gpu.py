@@ -26,8 +26,9 @@ def make_batch(seed, count, nmax, tmax):
     return specs
 
 
+@pytest.mark.parametrize("sched", ["persistent", "layered"])
 @pytest.mark.parametrize("mode", ["exact", "fma"])
-def test_batch_matches_oracle(mode):
+def test_batch_matches_oracle(mode, sched):
     specs = make_batch(7, 40, 300, 23)
     grids, hosts, entries = [], [], []
     for i, (name, n, T) in enumerate(specs):
@@ -45,7 +46,7 @@ def test_batch_matches_oracle(mode):
         grids.append(g)
         hosts.append((A, coef))
         entries.append((g, T, coef))
-    b = capi.Batch(entries, fp_mode=mode)
+    b = capi.Batch(entries, fp_mode=mode, mode=sched)
     st = b.stats()
     assert st.grids == len(specs)
     s = torch.cuda.current_stream()
