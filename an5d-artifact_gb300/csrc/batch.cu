@@ -427,9 +427,187 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
   return GBS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Batched run without allocation, for callers that may not allocate device
+// memory. Its scratch (grid table, work list, counters, error word) lives in
+// a static device array of this unit, its host staging in static host
+// arrays: nothing is allocated per call, on the device or the host.
+// ---------------------------------------------------------------------------
+namespace gbs {
+namespace noalloc {
+namespace {  // one copy per unit (exact and FMA mode each have their own)
+constexpr int kMaxGrids = GBS_NOALLOC_MAX_GRIDS;
+constexpr int kMaxItems = GBS_NOALLOC_MAX_ITEMS;
+
+struct Scratch {
+  GridDev grids[kMaxGrids];
+  Item items[kMaxItems];
+  unsigned counters[kMaxGrids + 1];  // [0] next item, [1 + g] items of grid g done
+  int err;                           // error bits of the kernel
+};
+
+// Held by every GPU that loads the library, until the process exits.
+static __device__ __align__(256) unsigned char scratch[sizeof(Scratch)];
+
+std::mutex mu;                       // one call at a time: one staging area
+GridDev h_grids[kMaxGrids];
+Item h_items[kMaxItems];
+void *dev_scratch[64];               // address of `scratch` per device
+
+// Time blocks of grid g: `full` blocks of degree bs, then single steps, with
+// as many blocks as T has parity (the same split as batch_blocks).
+void split_blocks(int T, int bs, int &full, int &single) {
+  full = T > 0 ? T / bs : 0;
+  single = T > 0 ? T - full * bs : 0;
+  if (T > 0 && ((full + single) - T) % 2 != 0 && full > 0) {
+    --full;
+    single += bs;
+  }
+}
+
+gbs_status run(const gbs_batch_grid *grids, int ngrids, cudaStream_t stream) {
+  if (!grids || ngrids <= 0) return fail(GBS_ERR_INVALID, "batch (no allocation): no grids");
+  if (ngrids > kMaxGrids)
+    return fail(GBS_ERR_INVALID, "batch (no allocation): %d grids, at most %d fit its static scratch", ngrids,
+                kMaxGrids);
+  std::lock_guard<std::mutex> lk(mu);
+  int kmax = 0;
+  for (int g = 0; g < ngrids; ++g) {
+    const gbs_batch_grid &bg = grids[g];
+    const gbs_stencil_def_t *s = stencil_def(bg.stencil);
+    if (!s || s->dim != 2) return fail(GBS_ERR_INVALID, "batch grid %d: not a 2-D stencil", g);
+    if (bg.n[0] < 1 || bg.n[1] < 1 || bg.timestep < 0 || !bg.dev_A)
+      return fail(GBS_ERR_INVALID, "batch grid %d: bad extent, timestep or buffer", g);
+    if (reinterpret_cast<uintptr_t>(bg.dev_A) % 128 != 0)
+      return fail(GBS_ERR_INVALID, "batch grid %d: buffer not 128-byte aligned", g);
+    gbs_desc d{};
+    d.stencil = bg.stencil;
+    d.dtype = GBS_F32;
+    d.n[0] = bg.n[0];
+    d.n[1] = bg.n[1];
+    d.n[2] = 1;
+    d.timestep = bg.timestep;
+    d.fp_mode = kFma ? GBS_FP_FMA : GBS_FP_EXACT;
+    const Layout L = make_layout(&d);
+    GridDev &x = h_grids[g];
+    std::memset(&x, 0, sizeof x);
+    x.base = static_cast<float *>(bg.dev_A);
+    x.pitch = L.pitch;
+    x.plane = L.plane;
+    x.d0 = L.dims[0];
+    x.d1 = L.dims[1];
+    x.shift = (int)L.shift;
+    x.sid = bg.stencil;
+    const int ni = L.dims[0] - 2 * s->rad;
+    x.sl = std::min(ni, 128);
+    x.nblocks = (ni + x.sl - 1) / x.sl;
+    const double div = bg.divisor != 0.0 ? bg.divisor : (double)s->divisor;
+    const bool fold = kFma && s->divisor && div != 0.0;
+    const int nt = s->kind == 1 ? 1 : s->nterms;
+    for (int t = 0; t < nt; ++t) {
+      const double c = bg.coef ? (double)((const float *)bg.coef)[t]
+                               : (s->kind == 1 ? (double)s->numerator : (double)s->terms[t].coef);
+      x.coef[t] = fold ? (float)(c / div) : (float)c;
+    }
+    x.div = (float)div;
+    x.rdiv = div_reciprocal<float>(div);
+    x.eps = (float)s->eps;
+    x.divmode = !s->divisor || fold ? 0 : (div_proven_exact(div) ? 2 : 1);
+    int full, single;
+    split_blocks(bg.timestep, family_degree(bg.stencil), full, single);
+    kmax = std::max(kmax, full + single);
+    for (int b : {family_degree(bg.stencil), 1}) {
+      gbs_status st = validate2d(L, geometry2d(L, b, x.sl, 0));
+      if (st != GBS_OK) return st;
+    }
+  }
+  // work items in time-block order, as the planned batch orders them
+  int nitems = 0;
+  int done_before[kMaxGrids] = {0};
+  for (int k = 0; k < kmax; ++k)
+    for (int sid = 0; sid < GBS_NUM_STENCILS; ++sid)
+      for (int g = 0; g < ngrids; ++g) {
+        if (grids[g].stencil != sid) continue;
+        const int bs = family_degree(sid);
+        int full, single;
+        split_blocks(grids[g].timestep, bs, full, single);
+        if (k >= full + single) continue;
+        const int b = k < full ? bs : 1;
+        const gbs_stencil_def_t *s = stencil_def(sid);
+        const int wout = ((128 - 2 * b * s->rad - 3) / 4) * 4;
+        const int nstrips = (h_grids[g].d1 - 2 * s->rad + wout - 1) / wout;
+        const int count = nstrips * h_grids[g].nblocks;
+        if (nitems + count > kMaxItems)
+          return fail(GBS_ERR_INVALID,
+                      "batch (no allocation): more than %d work items do not fit its static scratch "
+                      "(use gbs_batch_plan for larger batches)",
+                      kMaxItems);
+        for (int blk = 0; blk < h_grids[g].nblocks; ++blk)
+          for (int st = 0; st < nstrips; ++st) h_items[nitems++] = Item{g, k, b, st, blk, done_before[g], 0, 0};
+        done_before[g] += count;
+      }
+  if (nitems == 0) return GBS_OK;
+
+  // set-up, once per device, with that device current: the device address
+  // of the static scratch (its name in host code is only a stand-in)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "batch (no allocation): cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(GBS_ERR_NODEVICE, "device ordinal %d unsupported", dev);
+  if (!dev_scratch[dev]) {
+    void *ptr = nullptr;
+    if ((e = cudaGetSymbolAddress(&ptr, scratch)) != cudaSuccess)
+      return cuda_fail(e, "batch (no allocation): cudaGetSymbolAddress");
+    dev_scratch[dev] = ptr;
+  }
+  Scratch *sc = static_cast<Scratch *>(dev_scratch[dev]);
+
+  // stage the tables, clear the counters and the error word
+  if ((e = cudaMemcpyAsync(sc->grids, h_grids, sizeof(GridDev) * ngrids, cudaMemcpyHostToDevice, stream)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(sc->items, h_items, sizeof(Item) * nitems, cudaMemcpyHostToDevice, stream)) !=
+          cudaSuccess ||
+      (e = cudaMemsetAsync(sc->counters, 0, sizeof(unsigned) * (ngrids + 1), stream)) != cudaSuccess ||
+      (e = cudaMemsetAsync(&sc->err, 0, sizeof(int), stream)) != cudaSuccess)
+    return cuda_fail(e, "batch (no allocation): staging");
+  Args a{};
+  a.grids = sc->grids;
+  a.items = sc->items;
+  a.nitems = nitems;
+  a.next = sc->counters;
+  a.done = sc->counters + 1;
+  a.err = &sc->err;
+  const size_t smem = (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t)) + (size_t)kWpc * kParamSlot;
+  int per_sm = 0, sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch2d_kernel, kWpc * 32, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  (void)cudaGetLastError();
+  const int ctas = std::max(1, std::min(per_sm * std::max(sms, 1), (nitems + kWpc - 1) / kWpc));
+  batch2d_kernel<<<ctas, kWpc * 32, smem, stream>>>(a);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "batch (no allocation): launch");
+  // wait, and turn the kernel's error bits into a status
+  int herr = 0;
+  if ((e = cudaMemcpyAsync(&herr, &sc->err, sizeof(int), cudaMemcpyDeviceToHost, stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(stream)) != cudaSuccess)
+    return cuda_fail(e, "batch (no allocation): completion");
+  if (herr) return fail(GBS_ERR_TIMEOUT, "batch (no allocation): a device-side wait gave up (bits 0x%x)", herr);
+  return GBS_OK;
+}
+}  // namespace
+}  // namespace noalloc
+}  // namespace gbs
+
+extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_run_noalloc)(const gbs_batch_grid *grids, int ngrids,
+                                                             cudaStream_t stream) {
+  return gbs::noalloc::run(grids, ngrids, stream);
+}
+
 #if GBS_FMA
 // The C ABI entry points live in the FMA unit; they dispatch on fp_mode.
 extern "C++" gbs_status gbs_batch_build_0(const gbs_batch_grid *, int, int, gbs_batch **);
+extern "C++" gbs_status gbs_batch_run_noalloc_0(const gbs_batch_grid *, int, cudaStream_t);
 
 extern "C" {
 gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, int mode,
@@ -464,6 +642,12 @@ gbs_status gbs_batch_info(const gbs_batch *plan, gbs_batch_stats *out) {
   out->kernels = h->kernels;
   out->mode = h->mode;
   return GBS_OK;
+}
+
+gbs_status gbs_batch_run_noalloc(const gbs_batch_grid *grids, int ngrids, int fp_mode, void *stream) {
+  if (fp_mode == GBS_FP_FMA) return gbs_batch_run_noalloc_1(grids, ngrids, (cudaStream_t)stream);
+  if (fp_mode == GBS_FP_EXACT) return gbs_batch_run_noalloc_0(grids, ngrids, (cudaStream_t)stream);
+  return fail(GBS_ERR_INVALID, "bad fp_mode");
 }
 
 void gbs_batch_destroy(gbs_batch *plan) {

@@ -82,6 +82,8 @@ SIGNATURES = [
     ("gbs_batch_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_batch_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchStats)]),
     ("gbs_batch_destroy", None, [ctypes.c_void_p]),
+    ("gbs_batch_run_noalloc", ctypes.c_int, [ctypes.POINTER(BatchGrid), ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_void_p]),
     ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gbs_check_division", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_longlong,
                                           ctypes.POINTER(ctypes.c_longlong)]),
@@ -230,6 +232,23 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def batch_run_noalloc(grids, fp_mode="fma", stream: int = 0):
+    """gbs_batch_run_noalloc over (DeviceGrid, timestep, coef or None)
+    entries: the batched run that allocates no memory itself."""
+    arr = (BatchGrid * len(grids))()
+    keep = []
+    for i, (g, T, coef) in enumerate(grids):
+        arr[i].stencil = stencil_id(g.name)
+        arr[i].n[0], arr[i].n[1] = int(g.n[0]), int(g.n[1])
+        arr[i].timestep = int(T)
+        arr[i].dev_A = g.buf.data_ptr()
+        if coef is not None:
+            c = np.ascontiguousarray(coef, dtype=np.float32)
+            keep.append(c)
+            arr[i].coef = c.ctypes.data
+    check(lib().gbs_batch_run_noalloc(arr, len(grids), FP_MODES[fp_mode], ctypes.c_void_p(stream)))
 
 
 def measure_fp_peak(dtype) -> float:

@@ -178,6 +178,29 @@ gbs_status gbs_batch_run(gbs_batch *plan, void *stream);
 gbs_status gbs_batch_info(const gbs_batch *plan, gbs_batch_stats *out);
 void gbs_batch_destroy(gbs_batch *plan);
 
+/* Batched run that allocates nothing, for callers that may not allocate
+ * device memory: code that lives inside a framework whose caching allocator
+ * owns the whole device budget, or a host loop that must not call cudaMalloc
+ * (it can synchronise the device and stall other work). No counterpart in
+ * the artifact.
+ *
+ * Same result as gbs_batch_plan + gbs_batch_run with GBS_BATCH_PERSISTENT on
+ * the same grids. The grid table, work list and counters live in a static
+ * device array of about GBS_NOALLOC_MAX_ITEMS*32 bytes per fp mode (about
+ * 1 MB each), which every GPU that loads the library holds until the process
+ * exits; host staging uses static host arrays. Batches of more than
+ * GBS_NOALLOC_MAX_GRIDS grids or GBS_NOALLOC_MAX_ITEMS work items are
+ * rejected with GBS_ERR_INVALID. The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. Every call reuses the same array (its counters and
+ * error word are cleared on each call), so calls that overlap on the GPU
+ * race; calls from one process are serialised, and each call returns after
+ * its work has finished on `stream`, reporting device-side timeouts as
+ * GBS_ERR_TIMEOUT. dtype is GBS_F32. */
+#define GBS_NOALLOC_MAX_GRIDS 64
+#define GBS_NOALLOC_MAX_ITEMS 32768
+gbs_status gbs_batch_run_noalloc(const gbs_batch_grid *grids, int ngrids, int fp_mode, void *stream);
+
 /* Measures the device's fused multiply-add throughput in GFLOP/s (2 flops per
  * FMA): the FP term of the temporally-blocked stencil roofline. */
 gbs_status gbs_measure_fp_peak(int dtype, double *gflops);
