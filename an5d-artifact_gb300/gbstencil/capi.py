@@ -84,6 +84,11 @@ SIGNATURES = [
     ("gbs_batch_destroy", None, [ctypes.c_void_p]),
     ("gbs_batch_run_noalloc", ctypes.c_int, [ctypes.POINTER(BatchGrid), ctypes.c_int, ctypes.c_int,
                                              ctypes.c_void_p]),
+    ("gbs_adjoint_workspace", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    ("gbs_adjoint_forward", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
+    ("gbs_adjoint_backward", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gbs_check_division", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_longlong,
                                           ctypes.POINTER(ctypes.c_longlong)]),

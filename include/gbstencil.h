@@ -201,6 +201,26 @@ void gbs_batch_destroy(gbs_batch *plan);
 #define GBS_NOALLOC_MAX_ITEMS 32768
 gbs_status gbs_batch_run_noalloc(const gbs_batch_grid *grids, int ngrids, int fp_mode, void *stream);
 
+/* ---- adjoint (gradient of the time loop) -------------------------------- */
+/* No counterpart in the artifact, which only runs the forward loop. With
+ * checkpoints every C steps: gbs_adjoint_forward advances dev_A (engine
+ * layout, two planes) by d->timestep steps, saving u_0, u_C, u_2C, ... in the
+ * caller-provided workspace (gbs_adjoint_workspace bytes, 256-byte aligned);
+ * on return both planes hold u_T. gbs_adjoint_backward takes dL/du_T (one
+ * plane, engine layout; its halo is ignored) and writes dL/du_0 (one plane:
+ * interior and halo, since the fixed halo feeds every step) and, if
+ * dev_coef_grad is not NULL, dL/dc_k (device doubles, one per term, for the
+ * coefficients as the source writes them, before a divisor; stencils of at
+ * most 32 terms; gradient2d: one value, for its numerator). gradient2d uses
+ * its linearised update. Each chunk's
+ * states are recomputed from its checkpoint. Both calls are asynchronous on
+ * `stream`. */
+gbs_status gbs_adjoint_workspace(const gbs_desc *d, int checkpoint_every, size_t *bytes);
+gbs_status gbs_adjoint_forward(const gbs_desc *d, void *dev_A, int checkpoint_every, void *workspace,
+                               void *stream);
+gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *dev_grad_u0, double *dev_coef_grad,
+                                int checkpoint_every, void *workspace, void *stream);
+
 /* Measures the device's fused multiply-add throughput in GFLOP/s (2 flops per
  * FMA): the FP term of the temporally-blocked stencil roofline. */
 gbs_status gbs_measure_fp_peak(int dtype, double *gflops);
