@@ -57,6 +57,29 @@ BATCH_MIX = ["star2d1r", "star2d2r", "star2d3r", "star2d4r", "box2d1r", "box2d2r
              "j2d5pt", "j2d9pt"]
 
 
+# DRAM bytes (read + write) per interior cell per launch of the dominant
+# kernels, from ncu captures of small cases (dram__bytes_read.sum +
+# dram__bytes_write.sum over the interior cells of that case); the summaries
+# under profiles/ give the captures. Keyed by (stencil, dtype, bt).
+NCU_DRAM_BYTES_PER_CELL = {}
+
+
+def select_work(args):
+    """The workload's grids, narrowed by --only and resized by --n / --T
+    (used for small profiling cases of one kernel)."""
+    work = list(WORKLOADS[args.workload])
+    if args.only:
+        keep = {tuple(x.split(":")) for x in args.only.split(",")}
+        work = [w for w in work if (w[0], np.dtype(w[1]).name) in keep]
+        if not work:
+            raise SystemExit(f"--only {args.only!r} selects no grid of workload {args.workload}")
+    if args.n:
+        work = [(a, b, args.n, d) for a, b, c, d in work]
+    if args.T:
+        work = [(a, b, c, args.T) for a, b, c, d in work]
+    return work
+
+
 def batched_specs(count=512, seed=20250101, tmax=512):
     rng = np.random.default_rng(seed)
     out = []
@@ -147,7 +170,7 @@ def run_ours(args, rank, world):
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
-    work = WORKLOADS[args.workload]
+    work = select_work(args)
     grids, coefs, plans = [], [], []
     for i, (name, dt, n, T) in enumerate(work):
         g = DeviceGrid(name, dt, n, device=dev)
@@ -207,13 +230,14 @@ def run_ours(args, rank, world):
         for g, h, c, (_, _, _, T) in zip(grids, hosts, coefs, work):
             d, keep = capi.make_desc(g.name, g.dtype, g.n, T, args.fp_mode, coef=c)
             capi.run_host(d, h.numpy())
-    e2e_step()  # allocates gbs_run's device buffer once
-    torch.cuda.synchronize()
-    e2e_steps = max(1, min(args.steps, 2))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    if not args.no_e2e:
+        e2e_step()  # allocates gbs_run's device buffer once
+        torch.cuda.synchronize()
+        e2e_steps = max(1, min(args.steps, 2))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     h2d = sum(int(h.numel()) * h.element_size() for h in hosts)
     d2h = h2d
 
@@ -229,6 +253,12 @@ def run_ours(args, rank, world):
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     fp_peak = {np.dtype(np.float32): capi.measure_fp_peak(np.float32),
                np.dtype(np.float64): capi.measure_fp_peak(np.float64)}
+    fpp = capi.info(name)["fpp"]
+    # FP rate of the dominant kernel: algorithmic flops (fpp per cell update,
+    # bt updates per cell per launch) over the launch time
+    fp_achieved = fpp * p.bt * ncell / (launch_ms * 1e-3) / 1e9
+    per_cell = NCU_DRAM_BYTES_PER_CELL.get((name, np.dtype(dt).name, p.bt))
+    traffic = None if per_cell is None else int(per_cell * ncell)
     per = []
     for i, (nm, d_, n_, T_) in enumerate(work):
         ms = per_grid_ms[i] / args.steps
@@ -253,12 +283,16 @@ def run_ours(args, rank, world):
                    "fp_mode": args.fp_mode, "l2": "flushed between timed steps (512 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "per_stencil": per,
-        "e2e": {"value": round(cells * world / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GCells/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": None if args.no_e2e else {
+            "value": round(cells * world / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GCells/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None,
-                     "kernel": f"{name} {np.dtype(dt).name} bt={p.bt}",
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"},
+                     "frac": round(achieved / hbm, 4), "traffic": traffic,
+                     "kernel": f"{name} {np.dtype(dt).name} bt={p.bt}, {p.launches} launches of {ncell} cells",
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                     "fp": {"achieved_gflops": round(fp_achieved, 1), "peak_gflops": round(fp_peak[np.dtype(dt)], 1),
+                            "frac": round(fp_achieved / fp_peak[np.dtype(dt)], 4),
+                            "flops_per_cell_update": fpp, "peak_source": "gbs_measure_fp_peak (FMA loop)"}},
         "fp_peak_gflops": {k.name: round(v, 1) for k, v in fp_peak.items()},
         "clocks": clk.summary(),
         "gpu_launches": launches,
@@ -276,7 +310,8 @@ def cpu_sample(work, budget_s=12.0, threads=None):
     cells, secs, parts = 0, 0.0, []
     per_budget = budget_s / len(work)
     for i, (name, dt, n, T) in enumerate(work):
-        A = np.empty((2,) + tuple([n + 2 * po.BY_NAME[name][1]["rad"]] * po.BY_NAME[name][1]["dim"]), dt)
+        shape, nn = po.grid_shape(name, n)
+        A = np.empty(shape, dt)
         rng = np.random.default_rng(20250101 + i)
         A[0] = rng.random(A.shape[1:], dtype=np.float64 if dt == np.float64 else np.float32)
         A[1] = A[0]
@@ -285,16 +320,27 @@ def cpu_sample(work, budget_s=12.0, threads=None):
         ms1 = po.timed_run(name, A, n, 1, coef=c)
         Ts = int(max(1, min(T, per_budget * 1e3 / max(ms1, 1e-3))))
         ms = po.timed_run(name, A, n, Ts, coef=c)
-        ncell = n ** po.BY_NAME[name][1]["dim"]
+        ncell = int(np.prod(nn))
         cells += ncell * Ts
         secs += ms * 1e-3
-        parts.append(f"{name} {np.dtype(dt).name} {n}^{po.BY_NAME[name][1]['dim']} T={Ts}")
+        parts.append(f"{name} {np.dtype(dt).name} {'x'.join(map(str, nn))} T={Ts}")
     return cells / secs / 1e9, "; ".join(parts)
+
+
+def batched_cpu_work(args, count=16):
+    """A bounded sample of the batched workload for the CPU legs: its first
+    ``count`` grids (fp32), each at its own stencil and size."""
+    specs = batched_specs(args.batch_grids, tmax=args.batch_tmax)[:count]
+    return [(name, np.float32, n, T) for name, n, T in specs]
+
+
+def cpu_work(args):
+    return batched_cpu_work(args) if args.workload == "batched" else select_work(args)
 
 
 def run_reference(args, rank, world):
     import pyoracle as po
-    work = WORKLOADS[args.workload]
+    work = cpu_work(args)
     threads = po.max_threads()
     vals = []
     for _ in range(args.warmup):
@@ -312,7 +358,8 @@ def run_reference(args, rank, world):
         "data": "synthetic U[0,1) grids and normalised U[0,1) coefficients, seeded",
         "config": {"workload": args.workload, "grids": [f"{w[0]} {np.dtype(w[1]).name} {w[2]} T={w[3]}" for w in work]},
         "cpu_baseline": {"value": round(value, 4), "unit": "GCells/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample + ("; the first 16 grids of the batched workload"
+                                             if args.workload == "batched" else "")},
         "e2e": {"value": round(value, 4), "unit": "GCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -437,6 +484,10 @@ def main():
     ap.add_argument("--workload", default="suite3d", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--fp-mode", default="fma", choices=["fma", "exact"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--only", default="", help="grids of the workload to keep, e.g. box3d1r:float64")
+    ap.add_argument("--n", type=int, default=0, help="interior side length override")
+    ap.add_argument("--T", type=int, default=0, help="timestep override")
     ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
     ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "layered"],
@@ -454,9 +505,9 @@ def main():
         torch.distributed.init_process_group("nccl")
     line = run_batched(args, rank, world) if args.workload == "batched" else run_ours(args, rank, world)
     if rank == 0:
-        if not args.no_cpu and args.workload != "batched":
+        if not args.no_cpu:
             import pyoracle as po
-            v, sample = cpu_sample(WORKLOADS[args.workload])
+            v, sample = cpu_sample(cpu_work(args))
             line["cpu_baseline"] = {"value": round(v, 4), "unit": "GCells/s", "cores": po.max_threads(),
                                     "kind": "port", "sample": sample}
         print(json.dumps(line))
