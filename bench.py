@@ -61,7 +61,10 @@ BATCH_MIX = ["star2d1r", "star2d2r", "star2d3r", "star2d4r", "box2d1r", "box2d2r
 # kernels, from ncu captures of small cases (dram__bytes_read.sum +
 # dram__bytes_write.sum over the interior cells of that case); the summaries
 # under profiles/ give the captures. Keyed by (stencil, dtype, bt).
-NCU_DRAM_BYTES_PER_CELL = {}
+NCU_DRAM_BYTES_PER_CELL = {
+    ("box3d1r", "float64", 1): 15.74,   # 256^3 capture: 171.3 MB read + 92.8 MB written
+    ("star3d2r", "float32", 1): 8.20,   # 320^3 capture: 180.2 MB read + 88.4 MB written
+}
 
 
 def select_work(args):
