@@ -142,6 +142,15 @@ static int default_bt(const gbs_desc *d) {
   return std::max(1, std::min(bt, mx));
 }
 
+// bt and sl of the time loop for d: the caller's values, else the tuning
+// table's choice for this size, else the fixed rule above (sl 0: one wave)
+static void resolve_bt_sl(const gbs_desc *d, int *bt, int *sl) {
+  int tb = 0, ts = 0;
+  const bool tuned = (d->bt <= 0 || d->sl <= 0) && tuned_lookup(d, &tb, &ts);
+  *bt = d->bt > 0 ? d->bt : (tuned ? tb : default_bt(d));
+  *sl = d->sl > 0 ? d->sl : (tuned && tb == *bt ? ts : 0);
+}
+
 // Divisors for which the exhaustive self-test (every float input, see
 // gbs_check_division) shows the one-correction quotient equal to IEEE
 // division: the artifact's 118 and 159. The GPU test suite re-proves this.
@@ -349,7 +358,8 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
   if (pk.maxb == 0)
     return fail(GBS_ERR_UNSUPPORTED, "no kernels built for %s dtype=%d fp_mode=%d", s->name, d->dtype,
                 d->fp_mode);
-  int bt = d->bt > 0 ? d->bt : default_bt(d);
+  int bt = 0, sl = 0;
+  resolve_bt_sl(d, &bt, &sl);
   if (bt > pk.maxb)
     return fail(GBS_ERR_UNSUPPORTED, "bt=%d exceeds the largest fused degree built for %s (%d)", bt,
                 s->name, pk.maxb);
@@ -375,7 +385,7 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
     const void *src = base + (j % 2) * plane_bytes;
     void *dst = base + ((j + 1) % 2) * plane_bytes;
     if (s->dim == 2) {
-      Geometry2D g = geometry2d(L, b, d->sl, resident_warps_2d(d->stencil, d->dtype, fma, b));
+      Geometry2D g = geometry2d(L, b, sl, resident_warps_2d(d->stencil, d->dtype, fma, b));
       gbs_status st = validate2d(L, g);
       if (st != GBS_OK) return st;
       Launch2D a{};
@@ -399,7 +409,7 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
       cudaError_t e = pk.l2[b](a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");
     } else {
-      Geometry3D g = geometry3d(L, b, tile_rows_3d(d->stencil, d->dtype, fma, b), d->sl,
+      Geometry3D g = geometry3d(L, b, tile_rows_3d(d->stencil, d->dtype, fma, b), sl,
                                  resident_ctas_3d(d->stencil, d->dtype, fma, b));
       gbs_status st = validate3d(L, g);
       if (st != GBS_OK) return st;
@@ -487,13 +497,14 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
   const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
   const int mx = max_bt(d->stencil, d->dtype, fma);
   if (mx == 0) return fail(GBS_ERR_UNSUPPORTED, "no kernels built for %s", s->name);
-  const int bt = d->bt > 0 ? d->bt : default_bt(d);
+  int bt = 0, sl = 0;
+  resolve_bt_sl(d, &bt, &sl);
   if (bt > mx) return fail(GBS_ERR_UNSUPPORTED, "bt=%d exceeds the largest fused degree built (%d)", bt, mx);
   std::memset(out, 0, sizeof *out);
   out->bt = bt;
   out->launches = (int)split_steps(d->timestep, bt).size();
   if (s->dim == 2) {
-    Geometry2D g = geometry2d(L, bt, d->sl, resident_warps_2d(d->stencil, d->dtype, fma, bt));
+    Geometry2D g = geometry2d(L, bt, sl, resident_warps_2d(d->stencil, d->dtype, fma, bt));
     st = validate2d(L, g);
     if (st != GBS_OK) return st;
     out->bs1 = 4;
@@ -503,7 +514,7 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
     const double cols = 32.0 * L.V, rows = g.sl + 2.0 * bt * L.rad;
     out->redundancy = (cols * rows) / ((double)g.wout * g.sl);
   } else {
-    Geometry3D g = geometry3d(L, bt, tile_rows_3d(d->stencil, d->dtype, fma, bt), d->sl,
+    Geometry3D g = geometry3d(L, bt, tile_rows_3d(d->stencil, d->dtype, fma, bt), sl,
                                  resident_ctas_3d(d->stencil, d->dtype, fma, bt));
     st = validate3d(L, g);
     if (st != GBS_OK) return st;

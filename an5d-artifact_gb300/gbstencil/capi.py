@@ -90,6 +90,13 @@ SIGNATURES = [
     ("gbs_adjoint_backward", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("gbs_tune", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    ("gbs_tune_set", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    ("gbs_tune_lookup", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    ("gbs_tune_load", ctypes.c_int, [ctypes.c_char_p]),
+    ("gbs_tune_save", ctypes.c_int, [ctypes.c_char_p]),
+    ("gbs_tune_entries", ctypes.c_int, []),
+    ("gbs_tune_clear", None, []),
     ("gbs_check_division", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_longlong,
                                           ctypes.POINTER(ctypes.c_longlong)]),
     ("gbs_last_error", ctypes.c_char_p, []),
@@ -109,8 +116,17 @@ def lib():
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
+        # the tuning table measured on GB300 that ships with the package
+        table = Path(__file__).resolve().parent / "tuning_gb300.txt"
+        if table.exists():
+            check_with(L, L.gbs_tune_load(str(table).encode()))
         _lib = L
     return _lib
+
+
+def check_with(L, status: int):
+    if status != GBS_OK:
+        raise GbsError(status, L.gbs_last_error().decode())
 
 
 def check(status: int):

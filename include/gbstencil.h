@@ -124,6 +124,35 @@ gbs_status gbs_run_device(const gbs_desc *d, void *dev_A, void *stream);
 gbs_status gbs_get_layout(const gbs_desc *d, gbs_layout *out);
 gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out);
 
+/* ---- autotuner ---------------------------------------------------------- */
+/* Replaces the artifact's offline model (Model_V100.xlsm, Formula/Macro
+ * sheets) and its tuned-configuration lists (compiled/v100_float.csv:1-105,
+ * columns bS1,bS2,bT,sl). gbs_tune ranks every (bt, sl) the build supports
+ * for d's stencil, dtype, fp mode and size with a roofline model
+ * (max(2*sizeof(T)/(bt*B_hbm), redundancy*fpp/P_fp) per cell update, plus a
+ * launch gap per bt steps), times the candidates the model keeps on a scratch
+ * grid of the same size (d->timestep is ignored), records the fastest in the
+ * engine's tuning table and returns the candidates fastest first. When
+ * d->bt / d->sl are 0, the time loop and gbs_plan resolve them through that
+ * table (the entry of the same stencil, dtype and mode whose size class,
+ * floor(log2(interior cells)), is nearest, within 3), else by a fixed rule.
+ * The table is also loaded from the file named by the environment variable
+ * GBS_TUNING at first use. Text format, one entry per line:
+ * "<stencil> <f32|f64> <exact|fma> <size class> <bt> <sl> <ms per step>". */
+typedef struct gbs_tune_candidate {
+  int bt, sl;               /* sl 0: the engine's one-wave stream length */
+  double redundancy;        /* computed / useful cells per launch */
+  double model_ms_per_step; /* the model's time for one timestep */
+  double ms_per_step;       /* measured; < 0 if the model pruned it */
+} gbs_tune_candidate;
+gbs_status gbs_tune(const gbs_desc *d, gbs_tune_candidate *cands, int max_cands, int *ncands);
+gbs_status gbs_tune_set(const gbs_desc *d, int bt, int sl, double ms_per_step);
+gbs_status gbs_tune_lookup(const gbs_desc *d, int *bt, int *sl); /* bt = 0: no entry */
+gbs_status gbs_tune_load(const char *path);
+gbs_status gbs_tune_save(const char *path);
+int gbs_tune_entries(void);
+void gbs_tune_clear(void);
+
 /* Dense host grid <-> engine layout, both planes, enqueued on `stream`. */
 gbs_status gbs_upload(const gbs_desc *d, const void *host_A, void *dev_A, void *stream);
 gbs_status gbs_download(const gbs_desc *d, const void *dev_A, void *host_A, void *stream);
