@@ -308,7 +308,7 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
     x.sl = std::min(ni, 128);
     x.nblocks = (ni + x.sl - 1) / x.sl;
     const double div = bg.divisor != 0.0 ? bg.divisor : (double)s->divisor;
-    const bool fold = kFma && s->divisor && div != 0.0;
+    const bool fold = kFma && s->divisor;
     const int nt = s->kind == 1 ? 1 : s->nterms;
     for (int t = 0; t < nt; ++t) {
       double c = bg.coef ? (double)((const float *)bg.coef)[t]
@@ -502,7 +502,7 @@ gbs_status run(const gbs_batch_grid *grids, int ngrids, cudaStream_t stream) {
     x.sl = std::min(ni, 128);
     x.nblocks = (ni + x.sl - 1) / x.sl;
     const double div = bg.divisor != 0.0 ? bg.divisor : (double)s->divisor;
-    const bool fold = kFma && s->divisor && div != 0.0;
+    const bool fold = kFma && s->divisor;
     const int nt = s->kind == 1 ? 1 : s->nterms;
     for (int t = 0; t < nt; ++t) {
       const double c = bg.coef ? (double)((const float *)bg.coef)[t]

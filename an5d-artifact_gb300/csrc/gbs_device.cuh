@@ -222,11 +222,12 @@ __device__ __forceinline__ T term_next(T acc, T c, T a) {
 // gradient2d.c:17-21: u + num / sqrt(eps + sum_n (u - u_n)^2), evaluated as
 // C evaluates it: the differences and squares summed in T, each rounded, then
 // (since `1.0f / sqrt(x)` calls the double sqrt) the root, the quotient and
-// the final sum in double, rounded once to T. Both fp modes use this form:
-// the update amplifies rounding where neighbours agree, so even fusing the
-// squares drifts past the 1e-5 parity bound within ten steps, and the double
-// root and quotient dominate its cost either way.
-template <typename T, int NN>
+// the final sum in double, rounded once to T (exact mode). Both modes form
+// the sum of squares this way: the update amplifies rounding where
+// neighbours agree, so even fusing the squares drifts past the 1e-5 parity
+// bound within ten steps. FMA mode (FAST) replaces the double root and
+// quotient, which run on the FP64 pipe at 1/64 of the FP32 rate.
+template <typename T, int NN, bool FAST = false>
 __device__ __forceinline__ T gradient_update(T u, const T (&nb)[NN], T eps, T num) {
   using A = Arith<T>;
   T s = eps;
@@ -235,10 +236,31 @@ __device__ __forceinline__ T gradient_update(T u, const T (&nb)[NN], T eps, T nu
     const T d = A::sub(u, nb[n]);
     s = A::add(s, A::mul(d, d));
   }
-  const double q = __ddiv_rn((double)num, __dsqrt_rn((double)s));
-  const double r = __dadd_rn((double)u, q);
-  if constexpr (std::is_same<T, float>::value) return __double2float_rn(r);
-  else return r;
+  if constexpr (FAST && std::is_same<T, float>::value) {
+    // FMA mode, float: reciprocal square root in float (IEEE-rounded), no
+    // FP64 work. s is formed exactly as in exact mode.
+    return u + num * __frsqrt_rn(s);
+  } else if constexpr (FAST) {
+    // FMA mode, double: Newton-Raphson iteration for 1/sqrt(s),
+    // y <- y + y (1 - s y^2) / 2, from a single-precision estimate (relative
+    // error about 2^-22); each step squares the error, so two steps reach
+    // double precision with five FP64 operations instead of a division and
+    // a square root. Outside the guarded range: division and square root.
+    if (s >= 1e-30 && s <= 1e30) {
+      double y = (double)rsqrtf((float)s);
+      double h = fma(-s * y, y, 1.0);
+      y = fma(0.5 * y, h, y);
+      h = fma(-s * y, y, 1.0);
+      y = fma(0.5 * y, h, y);
+      return u + num * y;
+    }
+    return u + num / sqrt(s);
+  } else {
+    const double q = __ddiv_rn((double)num, __dsqrt_rn((double)s));
+    const double r = __dadd_rn((double)u, q);
+    if constexpr (std::is_same<T, float>::value) return __double2float_rn(r);
+    else return r;
+  }
 }
 
 // x / d, correctly rounded, for a divisor d known in advance with y =

@@ -154,7 +154,7 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
             if constexpr (di == 0) nb[t] = ext[R + e + dj];
             else nb[t] = win[wslot<UNR, W>(PH, R + di)][e];
           });
-          y[e] = gradient_update<T, ST::kTerms>(win[cslot][e], nb, p.eps, p.coef[0]);
+          y[e] = gradient_update<T, ST::kTerms, FMA>(win[cslot][e], nb, p.eps, p.coef[0]);
         });
       } else {
         // the direct form serves stencils whose off-centre rows are read at
@@ -175,7 +175,7 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
             else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
           });
         });
-        if constexpr (ST::kHasDiv) {
+        if constexpr (ST::kHasDiv && !FMA) {  // FMA mode: folded into the coefficients
 #pragma unroll
           for (int e = 0; e < V; ++e) y[e] = apply_div(y[e], p);
         }
@@ -212,7 +212,7 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
     constexpr int oslot = wslot<UNR, W>(PH, 0);
 #pragma unroll
     for (int e = 0; e < V; ++e) y[e] = win[oslot][e];
-    if constexpr (ST::kHasDiv) {
+    if constexpr (ST::kHasDiv && !FMA) {  // FMA mode: folded into the coefficients
 #pragma unroll
       for (int e = 0; e < V; ++e) y[e] = apply_div(y[e], p);
     }
@@ -455,8 +455,9 @@ cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
   p.nstrips = a.nstrips;
   p.nblocks = a.nblocks;
   p.sl = a.sl;
-  // FMA mode is tolerance-bound: a divisor is folded into the coefficients
-  const bool fold = FMA && ST::kHasDiv && a.div != 0.0;
+  // FMA mode is tolerance-bound: a divisor (nonzero, checked by the planner)
+  // is folded into the coefficients, and the kernel has no division at all
+  const bool fold = FMA && ST::kHasDiv;
   for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = fold ? (T)(a.coef[t] / a.div) : (T)a.coef[t];
   p.divmode = !ST::kHasDiv || fold ? 0 : (a.div_proven ? 2 : 1);
   p.div = (T)a.div;

@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(TJ * 32, 1)
         });
 #pragma unroll
         for (int e = 0; e < V; ++e) {
-          if constexpr (ST::kHasDiv) y[e] = apply_div3(acc[l][0][e], p);
+          if constexpr (ST::kHasDiv && !FMA) y[e] = apply_div3(acc[l][0][e], p);
           else y[e] = acc[l][0][e];
         }
         if (qhalo || jhalo || kedge) {
@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(TJ * 32, 1)
               else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
             });
           });
-          if constexpr (ST::kHasDiv) {
+          if constexpr (ST::kHasDiv && !FMA) {
 #pragma unroll
             for (int e = 0; e < V; ++e) y[e] = apply_div3(y[e], p);
           }
@@ -749,7 +749,7 @@ cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {
   p.ntj = a.ntj;
   p.nblocks = a.nblocks;
   p.sl = a.sl;
-  const bool fold = FMA && ST::kHasDiv && a.div != 0.0;
+  const bool fold = FMA && ST::kHasDiv;  // the divisor is nonzero (checked by the planner)
   for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = fold ? (T)(a.coef[t] / a.div) : (T)a.coef[t];
   p.divmode = !ST::kHasDiv || fold ? 0 : (a.div_proven ? 2 : 1);
   p.div = (T)a.div;

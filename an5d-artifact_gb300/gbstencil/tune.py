@@ -81,10 +81,14 @@ def main():
     ap.add_argument("--dtypes", default="float32,float64")
     ap.add_argument("--modes", default="fma,exact")
     ap.add_argument("--log", default="", help="also write every candidate's timing (JSON lines)")
+    ap.add_argument("--fresh", action="store_true",
+                    help="start from an empty table (default: re-tune into the shipped one)")
     args = ap.parse_args()
     import json
     names = args.stencils.split(",") if args.stencils else capi.NAMES
-    clear()
+    capi.lib()
+    if args.fresh:
+        clear()
     log = open(args.log, "w") if args.log else None
     for name in names:
         s = capi.info(name)
