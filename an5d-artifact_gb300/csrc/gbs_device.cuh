@@ -237,9 +237,24 @@ __device__ __forceinline__ T gradient_update(T u, const T (&nb)[NN], T eps, T nu
     s = A::add(s, A::mul(d, d));
   }
   if constexpr (FAST && std::is_same<T, float>::value) {
-    // FMA mode, float: reciprocal square root in float (IEEE-rounded), no
-    // FP64 work. s is formed exactly as in exact mode.
-    return u + num * __frsqrt_rn(s);
+    // FMA mode, float, all on the FP32 pipe. q = num / sqrt(s) as an
+    // unevaluated pair qh + ql: y0 = RN(1/sqrt(s)), then one Newton
+    // correction 1/sqrt(s) ~ y0 (1 + e/2) whose residual e = 1 - s y0^2 is
+    // formed exactly with FMA (s y0 = p + pe). u + qh + ql is then rounded
+    // once through Knuth's TwoSum, like exact mode's single rounding of the
+    // double sum (they differ only within ~2^-20 ulp of a rounding midpoint).
+    const float y0 = __frsqrt_rn(s);
+    const float p = __fmul_rn(s, y0);
+    const float pe = __fmaf_rn(s, y0, -p);
+    float e = __fmaf_rn(-p, y0, 1.0f);
+    e = __fmaf_rn(-pe, y0, e);
+    const float qh = __fmul_rn(num, y0);
+    const float qe = __fmaf_rn(num, y0, -qh);
+    const float ql = __fmaf_rn(qh, __fmul_rn(0.5f, e), qe);
+    const float t = __fadd_rn(u, qh);
+    const float bv = __fsub_rn(t, u);
+    const float err = __fadd_rn(__fsub_rn(u, __fsub_rn(t, bv)), __fsub_rn(qh, bv));
+    return __fadd_rn(t, __fadd_rn(err, ql));
   } else if constexpr (FAST) {
     // FMA mode, double: Newton-Raphson iteration for 1/sqrt(s),
     // y <- y + y (1 - s y^2) / 2, from a single-precision estimate (relative
