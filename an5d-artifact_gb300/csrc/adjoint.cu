@@ -3,25 +3,32 @@
 // No counterpart in the artifact: it differentiates the time loop that
 // kernel_stencil runs. For u_{t+1} = F(u_t) on the interior (halo fixed)
 // and a loss L(u_T) whose gradient lam_T = dL/du_T the caller supplies, it
-// returns dL/du_0 (interior and halo) and, for linear stencils, dL/dc_k for
-// the coefficients as the source writes them (before any divisor).
+// returns dL/du_0 (interior and halo) and, on request, dL/dc_k for the
+// coefficients as the source writes them (before any divisor).
+//
+// Linear stencils, u_{t+1}(x) = sum_k c_k u_t(x + o_k) / d:
+//  * lam_t(y) = sum_k c_k/d lam_{t+1}(y - o_k) on the interior, zero on the
+//    halo. Every offset set in the catalogue is symmetric (o in the set iff
+//    -o is), so this is the forward stencil with each coefficient moved to
+//    the mirrored offset: the engine's own kernels run it (FMA mode), one
+//    launch per step from one lam plane to the other.
+//  * a halo cell h feeds every step: dL/du_0(h) = sum_t sum_k c_k/d
+//    lam_{t+1}(h - o_k), accumulated by a kernel over the halo cells only.
+//  * dL/dc_k = sum_t sum_x lam_{t+1}(x) u_t(x + o_k) / d needs the forward
+//    states: only then are they recomputed (below), and a streaming kernel
+//    accumulates the products per thread and reduces them per CTA into a
+//    partial buffer (no atomics; summed in double at the end).
+// gradient2d, u_{t+1} = u + c q, q = (eps + s)^{-1/2}, s = sum_n (u - u_{x+n})^2:
+//    the linearised update, dF(x)/du(x) = 1 - c q^3 sum_n d_n(x),
+//    dF(x)/du(x+n) = c q^3 d_n(x), dF(x)/dc = q(x), evaluated on u_t: a
+//    pre-pass stores q and sum_n d_n per cell, a gather kernel applies the
+//    transposed Jacobian.
 //
 // Checkpointing: gbs_adjoint_forward advances the grid and saves u_t every
-// C steps into the caller's workspace; gbs_adjoint_backward walks the chunks
-// backwards, recomputes a chunk's C states from its checkpoint with the
-// forward engine itself (consecutive stash slots form the two-plane buffer
-// of a one-step launch), then runs the adjoint step kernel C times.
-//
-// Adjoint step (lam_{t+1} -> lam_t), with lam zero on the halo:
-//  * linear: lam_t(y) = sum_k c_k/d * lam_{t+1}(y - o_k) (the transposed
-//    stencil); at halo cells the same sum accumulates into the halo
-//    gradient, since a halo value feeds every step; dL/dc_k gains
-//    sum_x lam_{t+1}(x) u_t(x + o_k) / d, reduced per CTA into a partial
-//    buffer (no atomics; summed at the end in double).
-//  * gradient2d (u + c/sqrt(eps + s), s = sum_n (u - u_{x+n})^2): the
-//    linearised update, dF(x)/du(x) = 1 - c g(x) sum_n d_n(x),
-//    dF(x)/du(x+n) = c g(x) d_n(x), g = (eps + s)^{-3/2}, evaluated on u_t;
-//    dF(x)/dc = (eps + s)^{-1/2}.
+// C steps into the caller's workspace. When the states are needed,
+// gbs_adjoint_backward walks the chunks backwards and recomputes a chunk's C
+// states from its checkpoint with the forward engine (one launch per step,
+// each into its own stash slot), then runs the chunk's adjoint steps.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,10 +43,12 @@ namespace {
 
 constexpr int kAdjThreads = 256;
 constexpr int kMaxCoefGrad = 32;  // coefficient gradients for stencils of at most this many terms
+constexpr int kCoefBlocks = 1024;  // CTAs of the coefficient kernel (one partial row each)
 
 struct AdjGeom {
   long long pitch, plane;  // elements
   int d0, d1, d2, dim, shift, rad;
+  int rows, last;          // rows per plane (d0 or d0*d1), cells per row
   long long cells;         // d0*d1*d2
 };
 
@@ -48,142 +57,189 @@ __device__ __forceinline__ long long cell_off(const AdjGeom &g, int i, int j, in
                     : ((long long)i * g.d1 + j) * g.pitch + g.shift + k;
 }
 
-template <typename T, int NT> struct AdjParams {
-  AdjGeom g;
-  const T *u;          // u_t (one plane)
-  const T *lam_next;   // lam_{t+1}, zero on the halo
-  T *lam_prev;         // lam_t (interior written, halo zero)
-  T *halo_grad;        // dL/d(halo), accumulated
-  double *coef_part;   // [gridDim.x][NT] partial sums, accumulated
-  T coef[NT];          // c_k / divisor
-  T inv_div;           // 1 / divisor (1 without)
-  int want_coef;
+// (i, j) of row r; for 2-D rows j = 0 and the column is the second index
+__device__ __forceinline__ void row_ij(const AdjGeom &g, int r, int &i, int &j) {
+  if (g.dim == 2) {
+    i = r;
+    j = 0;
+  } else {
+    i = r / g.d1;
+    j = r - i * g.d1;
+  }
+}
+
+__device__ __forceinline__ bool row_interior(const AdjGeom &g, int i, int j) {
+  const int R = g.rad;
+  return i >= R && i < g.d0 - R && (g.dim == 2 || (j >= R && j < g.d1 - R));
+}
+
+// value of plane p at (i, j, c) (c the innermost index; 2-D: (i, c)); 0 off the grid
+template <typename T>
+__device__ __forceinline__ T ldz(const T *p, const AdjGeom &g, int i, int j, int c) {
+  if (i < 0 || i >= g.d0 || c < 0 || c >= g.last) return T(0);
+  if (g.dim == 2) return p[(long long)i * g.pitch + g.shift + c];
+  if (j < 0 || j >= g.d1) return T(0);
+  return p[((long long)i * g.d1 + j) * g.pitch + g.shift + c];
+}
+
+template <typename T, int NT> struct LinCoef {
+  T c[NT];  // c_k / d
 };
 
-template <typename T>
-__device__ __forceinline__ T ldz(const T *p, const AdjGeom &g, int i, int j, int k) {
-  if (i < 0 || i >= g.d0 || j < 0 || j >= g.d1 || (g.dim == 3 && (k < 0 || k >= g.d2))) return T(0);
-  return p[cell_off(g, i, j, k)];
-}
-
+// hg(h) += sum_k c_k/d lam(h - o_k) for every halo cell h. One warp per row:
+// every column of an all-halo row, the 2R edge columns of an interior row.
 template <class ST, typename T>
-__global__ void __launch_bounds__(kAdjThreads) adjoint_linear_kernel(const __grid_constant__ AdjParams<T, ST::kTerms> p) {
-  constexpr int NT = ST::kTerms;
-  constexpr int NP = NT <= kMaxCoefGrad ? NT : 1;
-  const AdjGeom &g = p.g;
-  const long long c = (long long)blockIdx.x * kAdjThreads + threadIdx.x;
-  T part[NP];
-#pragma unroll
-  for (int t = 0; t < NP; ++t) part[t] = T(0);
-  if (c < g.cells) {
-    int i, j, k = 0;
-    if (g.dim == 2) {
-      i = (int)(c / g.d1);
-      j = (int)(c % g.d1);
-    } else {
-      i = (int)(c / ((long long)g.d1 * g.d2));
-      const long long r = c % ((long long)g.d1 * g.d2);
-      j = (int)(r / g.d2);
-      k = (int)(r % g.d2);
-    }
-    const int R = g.rad;
-    const bool interior = i >= R && i < g.d0 - R && j >= R && j < g.d1 - R &&
-                          (g.dim == 2 || (k >= R && k < g.d2 - R));
-    T acc = T(0);
-    static_for<NT>([&](auto TI) {
-      constexpr int t = decltype(TI)::value;
-      constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
-      acc = fma(p.coef[t], ldz(p.lam_next, g, i - di, j - dj, k - dk), acc);
-    });
-    const long long o = cell_off(g, i, j, k);
-    if (interior) {
-      p.lam_prev[o] = acc;
-      if (p.want_coef && NT <= kMaxCoefGrad) {
-        const T l = p.lam_next[o];
-        static_for<NP>([&](auto TI) {
-          constexpr int t = decltype(TI)::value;
-          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
-          part[t] = l * p.u[cell_off(g, i + di, j + dj, k + dk)] * p.inv_div;
-        });
-      }
-    } else {
-      p.halo_grad[o] += acc;
-      p.lam_prev[o] = T(0);
-    }
-  }
-  if (NT <= kMaxCoefGrad && p.want_coef) {
-    // CTA sums of the NT products, added to this CTA's partial slot
-    __shared__ T red[kAdjThreads / 32][NP];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int t = 0; t < NP; ++t) {
-      T v = part[t];
-#pragma unroll
-      for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
-      if (lane == 0) red[w][t] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < NP) {
-      double s = 0.0;
-#pragma unroll
-      for (int ww = 0; ww < kAdjThreads / 32; ++ww) s += (double)red[ww][threadIdx.x];
-      p.coef_part[(size_t)blockIdx.x * NP + threadIdx.x] += s;
-    }
-  }
-}
-
-// gradient2d: linearised adjoint (2-D, radius 1)
-template <class ST, typename T>
-__global__ void __launch_bounds__(kAdjThreads) adjoint_gradient_kernel(const __grid_constant__ AdjParams<T, ST::kTerms> p, T eps, T num) {
-  const AdjGeom &g = p.g;
-  const long long c = (long long)blockIdx.x * kAdjThreads + threadIdx.x;
+__global__ void __launch_bounds__(kAdjThreads) halo_kernel(const __grid_constant__ AdjGeom g, const T *lam, T *hg,
+                                                           const __grid_constant__ LinCoef<T, ST::kTerms> cf) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * kAdjThreads + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * kAdjThreads) >> 5;
   const int R = g.rad;
-  auto inter = [&](int a, int b) { return a >= R && a < g.d0 - R && b >= R && b < g.d1 - R; };
-  // q(x) = (eps + s(x))^{-1/2} and sum_n d_n(x) for an interior cell x, in double
-  auto qfac = [&](int a, int b, double &sum_d) -> double {
-    const double ux = (double)p.u[cell_off(g, a, b, 0)];
-    double s = 0.0;
-    sum_d = 0.0;
-    static_for<ST::kTerms>([&](auto TI) {
-      constexpr int t = decltype(TI)::value;
-      const double dn = ux - (double)p.u[cell_off(g, a + ST::kOff[t][0], b + ST::kOff[t][1], 0)];
-      s = fma(dn, dn, s);
-      sum_d += dn;
-    });
-    return 1.0 / sqrt((double)eps + s);
-  };
-  double pnum = 0.0;  // d u_{t+1}(y) / d num = q(y), weighted by lam_{t+1}(y)
-  if (c < g.cells) {
-    const int i = (int)(c / g.d1), j = (int)(c % g.d1);
-    double acc = 0.0;
-    const bool yin = inter(i, j);
-    if (yin) {
-      double sd;
-      const double qy = qfac(i, j, sd);
-      const double ly = (double)p.lam_next[cell_off(g, i, j, 0)];
-      acc = ly * (1.0 - (double)num * qy * qy * qy * sd);
-      pnum = ly * qy;
+  for (int r = warp; r < g.rows; r += nwarps) {
+    int i, j;
+    row_ij(g, r, i, j);
+    const bool inner_row = row_interior(g, i, j);
+    const int ncols = inner_row ? 2 * R : g.last;
+    for (int q = lane; q < ncols; q += 32) {
+      const int c = inner_row ? (q < R ? q : g.last - 2 * R + q) : q;
+      T acc = T(0);
+      static_for<ST::kTerms>([&](auto TI) {
+        constexpr int t = decltype(TI)::value;
+        constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
+        // 2-D offsets are (row, column); 3-D (plane, row, column)
+        const T l = ST::kDim == 2 ? ldz(lam, g, i - di, 0, c - dj) : ldz(lam, g, i - di, j - dj, c - dk);
+        acc = fma(cf.c[t], l, acc);
+      });
+      const long long o = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift + c;
+      hg[o] += acc;
     }
-    const double uy = (double)p.u[cell_off(g, i, j, 0)];
+  }
+}
+
+// part[blockIdx.x][k] += sum over interior x of lam(x) u(x + o_k) / d.
+// One warp per interior row (grid-stride), products summed per thread in T,
+// reduced per CTA in double.
+template <class ST, typename T>
+__global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant__ AdjGeom g, const T *lam, const T *u,
+                                                           double *part, T inv_div) {
+  constexpr int NT = ST::kTerms;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int warp = (blockIdx.x * kAdjThreads + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * kAdjThreads) >> 5;
+  const int R = g.rad;
+  T acc[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) acc[t] = T(0);
+  for (int r = warp; r < g.rows; r += nwarps) {
+    int i, j;
+    row_ij(g, r, i, j);
+    if (!row_interior(g, i, j)) continue;
+    const long long row = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift;
+    for (int c = R + lane; c < g.last - R; c += 32) {
+      const T l = lam[row + c];
+      static_for<NT>([&](auto TI) {
+        constexpr int t = decltype(TI)::value;
+        constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
+        const long long o = ST::kDim == 2 ? (long long)di * g.pitch + dj
+                                          : ((long long)di * g.d1 + dj) * g.pitch + dk;
+        acc[t] = fma(l, u[row + c + o], acc[t]);
+      });
+    }
+  }
+  __shared__ double red[kAdjThreads / 32][NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    T v = acc[t];
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+    if (lane == 0) red[w][t] = (double)v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NT) {
+    double s = 0.0;
+#pragma unroll
+    for (int ww = 0; ww < kAdjThreads / 32; ++ww) s += red[ww][threadIdx.x];
+    part[(size_t)blockIdx.x * NT + threadIdx.x] += s * (double)inv_div;
+  }
+}
+
+// gradient2d pre-pass: for interior x, q(x) = (eps + s(x))^{-1/2} and
+// sd(x) = sum_n d_n(x), d_n = u(x) - u(x + n), from u_t (s formed as the
+// forward step forms it)
+template <class ST, typename T>
+__global__ void __launch_bounds__(kAdjThreads) grad_pre_kernel(const __grid_constant__ AdjGeom g, const T *u, T *qp,
+                                                               T *sdp, T eps) {
+  const long long cidx = (long long)blockIdx.x * kAdjThreads + threadIdx.x;
+  if (cidx >= g.cells) return;
+  const int i = (int)(cidx / g.d1), j = (int)(cidx - (long long)(cidx / g.d1) * g.d1);
+  const int R = g.rad;
+  if (!(i >= R && i < g.d0 - R && j >= R && j < g.d1 - R)) return;
+  using A = Arith<T>;
+  const long long o = cell_off(g, i, j, 0);
+  const T ux = u[o];
+  T s = eps;
+  double sd = 0.0;
+  static_for<ST::kTerms>([&](auto TI) {
+    constexpr int t = decltype(TI)::value;
+    const T d = A::sub(ux, u[cell_off(g, i + ST::kOff[t][0], j + ST::kOff[t][1], 0)]);
+    s = A::add(s, A::mul(d, d));
+    sd += (double)d;
+  });
+  // Newton-Raphson for 1/sqrt(s) from a single-precision estimate (two
+  // steps: relative error 2^-22 -> 2^-44 -> double precision)
+  const double sv = (double)s;
+  double y;
+  if (sv >= 1e-30 && sv <= 1e30) {
+    y = (double)rsqrtf((float)s);
+    double h = fma(-sv * y, y, 1.0);
+    y = fma(0.5 * y, h, y);
+    h = fma(-sv * y, y, 1.0);
+    y = fma(0.5 * y, h, y);
+  } else {
+    y = 1.0 / sqrt(sv);
+  }
+  qp[o] = (T)y;
+  sdp[o] = (T)sd;
+}
+
+// gradient2d adjoint step (transposed linearised Jacobian) and dL/dnum partials
+template <class ST, typename T>
+__global__ void __launch_bounds__(kAdjThreads) grad_adj_kernel(const __grid_constant__ AdjGeom g, const T *u,
+                                                               const T *qp, const T *sdp, const T *lam_next,
+                                                               T *lam_prev, T *hg, double *part, T num,
+                                                               int want_coef) {
+  const long long cidx = (long long)blockIdx.x * kAdjThreads + threadIdx.x;
+  const int R = g.rad;
+  double pnum = 0.0;
+  if (cidx < g.cells) {
+    const int i = (int)(cidx / g.d1), j = (int)(cidx - (long long)(cidx / g.d1) * g.d1);
+    auto inter = [&](int a, int b) { return a >= R && a < g.d0 - R && b >= R && b < g.d1 - R; };
+    const long long o = cell_off(g, i, j, 0);
+    const bool yin = inter(i, j);
+    T acc = T(0);
+    if (yin) {
+      const T q = qp[o], ly = lam_next[o];
+      acc = ly * (T(1) - num * q * q * q * sdp[o]);
+      pnum = (double)(ly * q);
+    }
+    const T uy = u[o];
     static_for<ST::kTerms>([&](auto TI) {
       constexpr int t = decltype(TI)::value;
       const int a = i - ST::kOff[t][0], b = j - ST::kOff[t][1];  // x with x + n = y
       if (a >= 0 && a < g.d0 && b >= 0 && b < g.d1 && inter(a, b)) {
-        double sd;
-        const double qx = qfac(a, b, sd);
-        const double dn = (double)p.u[cell_off(g, a, b, 0)] - uy;
-        acc += (double)p.lam_next[cell_off(g, a, b, 0)] * (double)num * qx * qx * qx * dn;
+        const long long ox = cell_off(g, a, b, 0);
+        const T qx = qp[ox];
+        acc = fma(lam_next[ox] * num * qx * qx * qx, u[ox] - uy, acc);
       }
     });
-    const long long o = cell_off(g, i, j, 0);
     if (yin) {
-      p.lam_prev[o] = (T)acc;
+      lam_prev[o] = acc;
     } else {
-      p.halo_grad[o] += (T)acc;
-      p.lam_prev[o] = T(0);
+      hg[o] += acc;
+      lam_prev[o] = T(0);
     }
   }
-  if (p.want_coef) {
+  if (want_coef) {
     __shared__ double red[kAdjThreads / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     double v = pnum;
@@ -195,7 +251,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_gradient_kernel(const __g
       double s = 0.0;
 #pragma unroll
       for (int ww = 0; ww < kAdjThreads / 32; ++ww) s += red[ww];
-      p.coef_part[blockIdx.x] += s;
+      part[blockIdx.x] += s;
     }
   }
 }
@@ -261,7 +317,7 @@ __global__ void sum_parts_kernel(const double *part, int nblocks, int nt, double
 struct Workspace {
   int ncp, C, nblocks, nt;
   size_t plane_bytes;
-  size_t off_cp, off_stash, off_lam, off_hg, off_part, total;
+  size_t off_cp, off_stash, off_lam, off_hg, off_q, off_sd, off_part, total;
 };
 
 Workspace workspace_of(const gbs_desc *d, const Layout &L, int C) {
@@ -272,13 +328,16 @@ Workspace workspace_of(const gbs_desc *d, const Layout &L, int C) {
   if (w.ncp < 1) w.ncp = 1;
   w.plane_bytes = (size_t)L.plane * L.esize;
   const long long cells = (long long)L.dims[0] * L.dims[1] * L.dims[2];
-  w.nblocks = (int)((cells + kAdjThreads - 1) / kAdjThreads);
-  w.nt = s->kind == 1 ? 1 : std::min(s->nterms, kMaxCoefGrad);
+  const bool grad = s->kind == 1;
+  w.nblocks = grad ? (int)((cells + kAdjThreads - 1) / kAdjThreads) : kCoefBlocks;
+  w.nt = grad ? 1 : std::min(s->nterms, kMaxCoefGrad);
   w.off_cp = 0;
   w.off_stash = w.off_cp + (size_t)w.ncp * w.plane_bytes;
   w.off_lam = w.off_stash + (size_t)C * w.plane_bytes;
   w.off_hg = w.off_lam + 2 * w.plane_bytes;
-  w.off_part = w.off_hg + w.plane_bytes;
+  w.off_q = w.off_hg + w.plane_bytes;
+  w.off_sd = w.off_q + (grad ? w.plane_bytes : 0);
+  w.off_part = w.off_sd + (grad ? w.plane_bytes : 0);
   w.total = w.off_part + (size_t)w.nblocks * w.nt * sizeof(double) + 256;
   return w;
 }
@@ -293,55 +352,109 @@ AdjGeom geom_of(const Layout &L) {
   g.dim = L.dim;
   g.shift = (int)L.shift;
   g.rad = L.rad;
+  g.rows = (int)L.rows;
+  g.last = L.dims[L.dim - 1];
   g.cells = (long long)L.dims[0] * L.dims[1] * L.dims[2];
   return g;
 }
 
-template <class ST, typename T>
-cudaError_t adjoint_step(const gbs_desc *d, const Layout &L, const void *u, const void *lam_next, void *lam_prev,
-                         void *hg, double *part, bool want_coef, cudaStream_t stream) {
+// coefficients of the forward update as the source writes them, divisor and eps
+void forward_coefficients(const gbs_desc *d, std::vector<double> &coef, double &div, double &eps) {
   const gbs_stencil_def_t *s = stencil_def(d->stencil);
-  AdjParams<T, ST::kTerms> p;
-  p.g = geom_of(L);
-  p.u = static_cast<const T *>(u);
-  p.lam_next = static_cast<const T *>(lam_next);
-  p.lam_prev = static_cast<T *>(lam_prev);
-  p.halo_grad = static_cast<T *>(hg);
-  p.coef_part = part;
-  const double div = d->divisor != 0.0 ? d->divisor : (double)s->divisor;
-  const double dv = s->divisor ? div : 1.0;
-  for (int t = 0; t < ST::kTerms; ++t) {
+  const int nt = s->kind == 1 ? 1 : s->nterms;
+  coef.assign(nt, 0.0);
+  for (int t = 0; t < nt; ++t) {
     double c;
-    if (s->kind == 1) c = d->coef ? (d->dtype == GBS_F64 ? ((const double *)d->coef)[0] : ((const float *)d->coef)[0])
-                                  : (double)s->numerator;
-    else c = d->coef ? (d->dtype == GBS_F64 ? ((const double *)d->coef)[t] : ((const float *)d->coef)[t])
-                     : (double)s->terms[t].coef;
-    p.coef[t] = (T)(s->kind == 1 ? c : c / dv);
+    if (d->coef) c = d->dtype == GBS_F64 ? ((const double *)d->coef)[t] : ((const float *)d->coef)[t];
+    else c = s->kind == 1 ? (double)s->numerator : (double)s->terms[t].coef;
+    coef[t] = c;
   }
-  p.inv_div = (T)(1.0 / dv);
-  p.want_coef = want_coef ? 1 : 0;
-  const unsigned blocks = (unsigned)((p.g.cells + kAdjThreads - 1) / kAdjThreads);
-  if constexpr (ST::kKind == KIND_GRADIENT) {
-    const T eps = (T)(d->eps != 0.0 ? d->eps : (double)s->eps);
-    adjoint_gradient_kernel<ST, T><<<blocks, kAdjThreads, 0, stream>>>(p, eps, p.coef[0]);
-  } else {
-    adjoint_linear_kernel<ST, T><<<blocks, kAdjThreads, 0, stream>>>(p);
-  }
-  return cudaGetLastError();
+  div = d->divisor != 0.0 ? d->divisor : (double)s->divisor;
+  eps = d->eps != 0.0 ? d->eps : (double)s->eps;
 }
 
-using AdjStepFn = cudaError_t (*)(const gbs_desc *, const Layout &, const void *, const void *, void *, void *,
-                                  double *, bool, cudaStream_t);
+// the forward coefficient of the mirrored offset, per term (linear stencils)
+bool transposed_coefficients(const gbs_stencil_def_t *s, const std::vector<double> &coef, std::vector<double> &out) {
+  out.assign(s->nterms, 0.0);
+  for (int t = 0; t < s->nterms; ++t) {
+    int m = -1;
+    for (int u = 0; u < s->nterms; ++u)
+      if (s->terms[u].di == -s->terms[t].di && s->terms[u].dj == -s->terms[t].dj &&
+          s->terms[u].dk == -s->terms[t].dk)
+        m = u;
+    if (m < 0) return false;
+    out[t] = coef[m];
+  }
+  return true;
+}
 
-AdjStepFn adj_step_fn(int sid, int dtype) {
+// kernels of one stencil and dtype
+struct AdjKernels {
+  cudaError_t (*halo)(const AdjGeom &, const void *, void *, const std::vector<double> &, double, cudaStream_t);
+  cudaError_t (*coef)(const AdjGeom &, const void *, const void *, double *, double, cudaStream_t);
+  cudaError_t (*grad)(const AdjGeom &, const void *, void *, void *, const void *, void *, void *, double *, double,
+                      double, bool, cudaStream_t);
+};
+
+unsigned row_grid(const AdjGeom &g) {
+  const long long warps = g.rows;
+  const long long blocks = (warps * 32 + kAdjThreads - 1) / kAdjThreads;
+  return (unsigned)std::max<long long>(1, std::min<long long>(blocks, 16384));
+}
+
+template <class ST, typename T>
+cudaError_t run_halo(const AdjGeom &g, const void *lam, void *hg, const std::vector<double> &coef, double div,
+                     cudaStream_t s) {
+  if constexpr (ST::kKind == KIND_GRADIENT) {
+    return cudaErrorInvalidValue;
+  } else {
+    LinCoef<T, ST::kTerms> cf;
+    const double dv = ST::kHasDiv ? div : 1.0;
+    for (int t = 0; t < ST::kTerms; ++t) cf.c[t] = (T)(coef[t] / dv);
+    halo_kernel<ST, T><<<row_grid(g), kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<T *>(hg), cf);
+    return cudaGetLastError();
+  }
+}
+
+template <class ST, typename T>
+cudaError_t run_coef(const AdjGeom &g, const void *lam, const void *u, double *part, double div, cudaStream_t s) {
+  if constexpr (ST::kKind == KIND_GRADIENT || ST::kTerms > kMaxCoefGrad) {
+    return cudaErrorInvalidValue;
+  } else {
+    const double dv = ST::kHasDiv ? div : 1.0;
+    coef_kernel<ST, T><<<kCoefBlocks, kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<const T *>(u),
+                                                           part, (T)(1.0 / dv));
+    return cudaGetLastError();
+  }
+}
+
+template <class ST, typename T>
+cudaError_t run_grad(const AdjGeom &g, const void *u, void *q, void *sd, const void *lam_next, void *lam_prev,
+                     void *hg, double *part, double num, double eps, bool want_coef, cudaStream_t s) {
+  if constexpr (ST::kKind != KIND_GRADIENT) {
+    return cudaErrorInvalidValue;
+  } else {
+    const unsigned blocks = (unsigned)((g.cells + kAdjThreads - 1) / kAdjThreads);
+    grad_pre_kernel<ST, T><<<blocks, kAdjThreads, 0, s>>>(g, static_cast<const T *>(u), static_cast<T *>(q),
+                                                          static_cast<T *>(sd), (T)eps);
+    grad_adj_kernel<ST, T><<<blocks, kAdjThreads, 0, s>>>(
+        g, static_cast<const T *>(u), static_cast<const T *>(q), static_cast<const T *>(sd),
+        static_cast<const T *>(lam_next), static_cast<T *>(lam_prev), static_cast<T *>(hg), part, (T)num,
+        want_coef ? 1 : 0);
+    return cudaGetLastError();
+  }
+}
+
+AdjKernels adj_kernels(int sid, int dtype) {
   switch (sid) {
-#define GBS_ADJ(id, S) \
-  case id:             \
-    return dtype == GBS_F64 ? &adjoint_step<S, double> : &adjoint_step<S, float>;
+#define GBS_ADJ(id, S)                                                                            \
+  case id:                                                                                         \
+    return dtype == GBS_F64 ? AdjKernels{&run_halo<S, double>, &run_coef<S, double>, &run_grad<S, double>} \
+                            : AdjKernels{&run_halo<S, float>, &run_coef<S, float>, &run_grad<S, float>};
     GBS_FOR_EACH_STENCIL(GBS_ADJ)
 #undef GBS_ADJ
     default:
-      return nullptr;
+      return AdjKernels{nullptr, nullptr, nullptr};
   }
 }
 
@@ -410,7 +523,8 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
   if (st != GBS_OK) return st;
   if (!dev_lamT || !dev_grad_u0) return fail(GBS_ERR_INVALID, "NULL lam_T or grad_u0");
   const gbs_stencil_def_t *sd = stencil_def(d->stencil);
-  if (dev_coef_grad && sd->kind != 1 && sd->nterms > kMaxCoefGrad)
+  const bool gradient = sd->kind == 1;
+  if (dev_coef_grad && !gradient && sd->nterms > kMaxCoefGrad)
     return fail(GBS_ERR_UNSUPPORTED, "coefficient gradients need at most %d terms", kMaxCoefGrad);
   int *err = nullptr;
   if ((st = error_word(&err)) != GBS_OK) return st;
@@ -419,12 +533,21 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
   const AdjGeom g = geom_of(L);
   char *ws = static_cast<char *>(workspace);
   cudaStream_t s = (cudaStream_t)stream;
-  AdjStepFn step = adj_step_fn(d->stencil, d->dtype);
+  const AdjKernels K = adj_kernels(d->stencil, d->dtype);
   const unsigned blocks = (unsigned)((g.cells + kAdjThreads - 1) / kAdjThreads);
   char *stash = ws + w.off_stash;
   char *lam[2] = {ws + w.off_lam, ws + w.off_lam + w.plane_bytes};
   char *hg = ws + w.off_hg;
   double *part = reinterpret_cast<double *>(ws + w.off_part);
+
+  std::vector<double> coef, coefT;
+  double div = 0.0, eps = 0.0;
+  forward_coefficients(d, coef, div, eps);
+  if (sd->divisor && div == 0.0) return fail(GBS_ERR_INVALID, "divisor must be nonzero");
+  if (!gradient && !transposed_coefficients(sd, coef, coefT))
+    return fail(GBS_ERR_UNSUPPORTED, "%s has an asymmetric offset set", sd->name);
+  gbs_desc dT = *d;  // the transposed step: the forward kernels, FMA mode
+  dT.fp_mode = GBS_FP_FMA;
 
   CK(cudaMemcpyAsync(lam[0], dev_lamT, w.plane_bytes, cudaMemcpyDeviceToDevice, s), "adjoint: lam_T");
   if (d->dtype == GBS_F64) zero_halo_kernel<double><<<blocks, kAdjThreads, 0, s>>>((double *)lam[0], g);
@@ -432,29 +555,48 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
   CK(cudaMemsetAsync(lam[1], 0, w.plane_bytes, s), "adjoint: memset");
   CK(cudaMemsetAsync(hg, 0, w.plane_bytes, s), "adjoint: memset");
   CK(cudaMemsetAsync(part, 0, (size_t)w.nblocks * w.nt * sizeof(double), s), "adjoint: memset");
-  // the halo of every stash slot: the fixed boundary (never rewritten)
-  for (int k = 0; k < w.C; ++k)
-    CK(cudaMemcpyAsync(stash + (size_t)k * w.plane_bytes, ws + w.off_cp, w.plane_bytes, cudaMemcpyDeviceToDevice, s),
-       "adjoint: stash");
   int cur = 0;
-  gbs_desc d1 = *d;
-  d1.timestep = 1;
-  d1.bt = 1;
-  d1.sl = 0;
-  for (int j = w.ncp - 1; j >= 0; --j) {
-    const int t0 = j * w.C;
-    const int c = std::min(w.C, d->timestep - t0);
-    if (c <= 0) continue;
-    // recompute u_{t0} .. u_{t0+c-1} into the stash
-    CK(cudaMemcpyAsync(stash, ws + w.off_cp + (size_t)j * w.plane_bytes, w.plane_bytes, cudaMemcpyDeviceToDevice, s),
-       "adjoint: restore");
-    for (int k = 1; k < c; ++k)
-      if ((st = run_loop(&d1, L, stash + (size_t)(k - 1) * w.plane_bytes, s, err)) != GBS_OK) return st;
-    // lam_{t+1} -> lam_t for t = t0+c-1 .. t0
-    for (int k = c - 1; k >= 0; --k) {
-      CK(step(d, L, stash + (size_t)k * w.plane_bytes, lam[cur], lam[cur ^ 1], hg, part, dev_coef_grad != nullptr, s),
-         "adjoint: step");
-      cur ^= 1;
+  // one adjoint step lam[cur] (= lam_{t+1}) -> lam[cur ^ 1] (= lam_t) on state u_t
+  auto step = [&](const char *u) -> gbs_status {
+    if (gradient) {
+      CK(K.grad(g, u, ws + w.off_q, ws + w.off_sd, lam[cur], lam[cur ^ 1], hg, part, coef[0], eps,
+                dev_coef_grad != nullptr, s),
+         "adjoint: gradient2d step");
+    } else {
+      CK(K.halo(g, lam[cur], hg, coef, div, s), "adjoint: halo");
+      if (dev_coef_grad) CK(K.coef(g, lam[cur], u, part, div, s), "adjoint: coefficients");
+      gbs_status r = launch_block(&dT, L, coefT.data(), div, eps, 0, 1, lam[cur], lam[cur ^ 1], s, err);
+      if (r != GBS_OK) return r;
+    }
+    cur ^= 1;
+    return GBS_OK;
+  };
+
+  if (!gradient && !dev_coef_grad) {
+    // no forward state enters: T transposed steps from lam_T
+    for (int t = d->timestep - 1; t >= 0; --t)
+      if ((st = step(nullptr)) != GBS_OK) return st;
+  } else {
+    // the halo of every stash slot: the fixed boundary (never rewritten)
+    for (int k = 0; k < w.C; ++k)
+      CK(cudaMemcpyAsync(stash + (size_t)k * w.plane_bytes, ws + w.off_cp, w.plane_bytes, cudaMemcpyDeviceToDevice,
+                         s),
+         "adjoint: stash");
+    for (int j = w.ncp - 1; j >= 0; --j) {
+      const int t0 = j * w.C;
+      const int c = std::min(w.C, d->timestep - t0);
+      if (c <= 0) continue;
+      // recompute u_{t0} .. u_{t0+c-1} into the stash, one launch per step
+      CK(cudaMemcpyAsync(stash, ws + w.off_cp + (size_t)j * w.plane_bytes, w.plane_bytes, cudaMemcpyDeviceToDevice,
+                         s),
+         "adjoint: restore");
+      for (int k = 1; k < c; ++k)
+        if ((st = launch_block(d, L, coef.data(), div, eps, 0, 1, stash + (size_t)(k - 1) * w.plane_bytes,
+                               stash + (size_t)k * w.plane_bytes, s, err)) != GBS_OK)
+          return st;
+      // lam_{t+1} -> lam_t for t = t0+c-1 .. t0
+      for (int k = c - 1; k >= 0; --k)
+        if ((st = step(stash + (size_t)k * w.plane_bytes)) != GBS_OK) return st;
     }
   }
   if (d->dtype == GBS_F64)

@@ -381,9 +381,24 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
   char *base = static_cast<char *>(dev_A);
   const size_t plane_bytes = (size_t)L.plane * L.esize;
   for (size_t j = 0; j < steps.size(); ++j) {
-    const int b = steps[j];
-    const void *src = base + (j % 2) * plane_bytes;
-    void *dst = base + ((j + 1) % 2) * plane_bytes;
+    gbs_status st = launch_block(d, L, coef.data(), div, eps, sl, steps[j], base + (j % 2) * plane_bytes,
+                                 base + ((j + 1) % 2) * plane_bytes, stream, err);
+    if (st != GBS_OK) return st;
+  }
+  return GBS_OK;
+}
+
+// One launch of b fused steps from plane src to plane dst (layout L; the
+// interior of dst is written, its halo never): coefficients as the source
+// writes them, divisor and eps resolved, sl 0 = one wave.
+gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, double div, double eps, int sl,
+                        int b, const void *src, void *dst, cudaStream_t stream, int *err) {
+  const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
+  const Picks &pk = picks(d->stencil, d->dtype, fma);
+  if (b < 1 || b > pk.maxb)
+    return fail(GBS_ERR_UNSUPPORTED, "no kernel of degree %d built for %s", b, s->name);
+  {
     if (s->dim == 2) {
       Geometry2D g = geometry2d(L, b, sl, resident_warps_2d(d->stencil, d->dtype, fma, b));
       gbs_status st = validate2d(L, g);
@@ -401,7 +416,7 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
       a.nstrips = g.nstrips;
       a.nblocks = g.nblocks;
       a.sl = g.sl;
-      a.coef = coef.data();
+      a.coef = coef;
       a.div = div;
       a.eps = eps;
       a.div_proven = d->dtype == GBS_F32 && div_proven_exact(div);
@@ -429,7 +444,7 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
       a.ntj = g.ntj;
       a.nblocks = g.nblocks;
       a.sl = g.sl;
-      a.coef = coef.data();
+      a.coef = coef;
       a.div = div;
       a.div_proven = d->dtype == GBS_F32 && div_proven_exact(div);
       if (!pk.l3[b]) return fail(GBS_ERR_UNSUPPORTED, "no 3-D kernel for b=%d", b);

@@ -47,6 +47,8 @@ long long resident_warps_2d(int sid, int dtype, int fma, int b);
 gbs_status validate2d(const Layout &L, const Geometry2D &g);
 gbs_status error_word(int **out);
 gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_t stream, int *err);
+gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, double div, double eps, int sl,
+                        int b, const void *src, void *dst, cudaStream_t stream, int *err);
 int max_bt(int sid, int dtype, int fma);
 // the tuning table's (bt, sl) for d's stencil, dtype, mode and size class
 bool tuned_lookup(const gbs_desc *d, int *bt, int *sl);
