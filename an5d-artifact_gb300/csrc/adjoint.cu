@@ -86,65 +86,83 @@ template <typename T, int NT> struct LinCoef {
   T c[NT];  // c_k / d
 };
 
-// hg(h) += sum_k c_k/d lam(h - o_k) for every halo cell h. One warp per row:
-// every column of an all-halo row, the 2R edge columns of an interior row.
+// hg(h) += sum_k c_k/d lam(h - o_k) for every halo cell h. Work units of
+// one warp: (row, 32-column segment) of an all-halo row, or the 2R edge
+// columns of an interior row (segment 0 only).
 template <class ST, typename T>
 __global__ void __launch_bounds__(kAdjThreads) halo_kernel(const __grid_constant__ AdjGeom g, const T *lam, T *hg,
                                                            const __grid_constant__ LinCoef<T, ST::kTerms> cf) {
   const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * kAdjThreads + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * kAdjThreads) >> 5;
+  const long long nseg = (g.last + 31) / 32;
+  const long long units = (long long)g.rows * nseg;
+  const long long nwarps = ((long long)gridDim.x * kAdjThreads) >> 5;
   const int R = g.rad;
-  for (int r = warp; r < g.rows; r += nwarps) {
+  for (long long u = ((long long)blockIdx.x * kAdjThreads + threadIdx.x) >> 5; u < units; u += nwarps) {
+    const int r = (int)(u / nseg), seg = (int)(u - (long long)r * nseg);
     int i, j;
     row_ij(g, r, i, j);
-    const bool inner_row = row_interior(g, i, j);
-    const int ncols = inner_row ? 2 * R : g.last;
-    for (int q = lane; q < ncols; q += 32) {
-      const int c = inner_row ? (q < R ? q : g.last - 2 * R + q) : q;
-      T acc = T(0);
-      static_for<ST::kTerms>([&](auto TI) {
-        constexpr int t = decltype(TI)::value;
-        constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
-        // 2-D offsets are (row, column); 3-D (plane, row, column)
-        const T l = ST::kDim == 2 ? ldz(lam, g, i - di, 0, c - dj) : ldz(lam, g, i - di, j - dj, c - dk);
-        acc = fma(cf.c[t], l, acc);
-      });
-      const long long o = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift + c;
-      hg[o] += acc;
+    int c;
+    if (row_interior(g, i, j)) {
+      if (seg != 0 || lane >= 2 * R) continue;
+      c = lane < R ? lane : g.last - 2 * R + lane;
+    } else {
+      c = seg * 32 + lane;
+      if (c >= g.last) continue;
     }
+    T acc = T(0);
+    static_for<ST::kTerms>([&](auto TI) {
+      constexpr int t = decltype(TI)::value;
+      constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
+      // 2-D offsets are (row, column); 3-D (plane, row, column)
+      const T l = ST::kDim == 2 ? ldz(lam, g, i - di, 0, c - dj) : ldz(lam, g, i - di, j - dj, c - dk);
+      acc = fma(cf.c[t], l, acc);
+    });
+    const long long o = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift + c;
+    hg[o] += acc;
   }
 }
 
 // part[blockIdx.x][k] += sum over interior x of lam(x) u(x + o_k) / d.
-// One warp per interior row (grid-stride), products summed per thread in T,
+// Work units of one warp: (interior row, 128-column segment), four
+// independent columns per lane in flight; products summed per thread in T,
 // reduced per CTA in double.
 template <class ST, typename T>
 __global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant__ AdjGeom g, const T *lam, const T *u,
                                                            double *part, T inv_div) {
   constexpr int NT = ST::kTerms;
+  constexpr int SEG = 128;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int warp = (blockIdx.x * kAdjThreads + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * kAdjThreads) >> 5;
   const int R = g.rad;
+  const int width = g.last - 2 * R;
+  const long long nseg = (width + SEG - 1) / SEG;
+  const long long units = (long long)g.rows * nseg;
+  const long long nwarps = ((long long)gridDim.x * kAdjThreads) >> 5;
   T acc[NT];
 #pragma unroll
   for (int t = 0; t < NT; ++t) acc[t] = T(0);
-  for (int r = warp; r < g.rows; r += nwarps) {
+  for (long long un = ((long long)blockIdx.x * kAdjThreads + threadIdx.x) >> 5; un < units; un += nwarps) {
+    const int r = (int)(un / nseg), seg = (int)(un - (long long)r * nseg);
     int i, j;
     row_ij(g, r, i, j);
     if (!row_interior(g, i, j)) continue;
     const long long row = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift;
-    for (int c = R + lane; c < g.last - R; c += 32) {
-      const T l = lam[row + c];
-      static_for<NT>([&](auto TI) {
-        constexpr int t = decltype(TI)::value;
-        constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
-        const long long o = ST::kDim == 2 ? (long long)di * g.pitch + dj
-                                          : ((long long)di * g.d1 + dj) * g.pitch + dk;
-        acc[t] = fma(l, u[row + c + o], acc[t]);
-      });
+    const int c0 = R + seg * SEG + lane;
+    T l[SEG / 32];
+    bool in[SEG / 32];
+#pragma unroll
+    for (int q = 0; q < SEG / 32; ++q) {
+      const int c = c0 + 32 * q;
+      in[q] = c < g.last - R;
+      l[q] = in[q] ? lam[row + c] : T(0);
     }
+    static_for<NT>([&](auto TI) {
+      constexpr int t = decltype(TI)::value;
+      constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
+      const long long o = ST::kDim == 2 ? (long long)di * g.pitch + dj : ((long long)di * g.d1 + dj) * g.pitch + dk;
+#pragma unroll
+      for (int q = 0; q < SEG / 32; ++q)
+        if (in[q]) acc[t] = fma(l[q], u[row + c0 + 32 * q + o], acc[t]);
+    });
   }
   __shared__ double red[kAdjThreads / 32][NT];
 #pragma unroll
@@ -396,10 +414,11 @@ struct AdjKernels {
                       double, bool, cudaStream_t);
 };
 
-unsigned row_grid(const AdjGeom &g) {
-  const long long warps = g.rows;
+// one warp per (row, 32-column segment), at most 65536 CTAs (grid-stride beyond)
+unsigned halo_grid(const AdjGeom &g) {
+  const long long warps = (long long)g.rows * ((g.last + 31) / 32);
   const long long blocks = (warps * 32 + kAdjThreads - 1) / kAdjThreads;
-  return (unsigned)std::max<long long>(1, std::min<long long>(blocks, 16384));
+  return (unsigned)std::max<long long>(1, std::min<long long>(blocks, 65536));
 }
 
 template <class ST, typename T>
@@ -411,7 +430,7 @@ cudaError_t run_halo(const AdjGeom &g, const void *lam, void *hg, const std::vec
     LinCoef<T, ST::kTerms> cf;
     const double dv = ST::kHasDiv ? div : 1.0;
     for (int t = 0; t < ST::kTerms; ++t) cf.c[t] = (T)(coef[t] / dv);
-    halo_kernel<ST, T><<<row_grid(g), kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<T *>(hg), cf);
+    halo_kernel<ST, T><<<halo_grid(g), kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<T *>(hg), cf);
     return cudaGetLastError();
   }
 }
