@@ -86,40 +86,82 @@ template <typename T, int NT> struct LinCoef {
   T c[NT];  // c_k / d
 };
 
-// hg(h) += sum_k c_k/d lam(h - o_k) for every halo cell h. Work units of
-// one warp: (row, 32-column segment) of an all-halo row, or the 2R edge
-// columns of an interior row (segment 0 only).
+// Halo cells, enumerated without touching the interior:
+//  A: the 2R edge columns of every interior row, one thread per cell;
+//  B: every cell of the all-halo rows, one warp per 32-column segment.
+// All-halo rows: 2-D rows i < R or i >= d0 - R; 3-D the planes i < R or
+// i >= d0 - R (every row j), then the rows j < R or j >= d1 - R of each
+// interior plane.
+struct HaloPlan {
+  long long na;      // A cells, rounded up to whole warps
+  long long rows_b;  // all-halo rows
+  int nseg;          // 32-column segments per row
+};
+
+__host__ __device__ inline HaloPlan halo_plan(const AdjGeom &g) {
+  HaloPlan h{};
+  const int R = g.rad;
+  const long long inner_rows = g.dim == 2 ? (long long)(g.d0 - 2 * R) : (long long)(g.d0 - 2 * R) * (g.d1 - 2 * R);
+  h.na = (inner_rows * 2 * R + 31) / 32 * 32;
+  h.rows_b = (long long)g.rows - inner_rows;
+  h.nseg = (g.last + 31) / 32;
+  return h;
+}
+
+// hg(h) += sum_k c_k/d lam(h - o_k) for every halo cell h
 template <class ST, typename T>
 __global__ void __launch_bounds__(kAdjThreads) halo_kernel(const __grid_constant__ AdjGeom g, const T *lam, T *hg,
                                                            const __grid_constant__ LinCoef<T, ST::kTerms> cf) {
-  const int lane = threadIdx.x & 31;
-  const long long nseg = (g.last + 31) / 32;
-  const long long units = (long long)g.rows * nseg;
-  const long long nwarps = ((long long)gridDim.x * kAdjThreads) >> 5;
+  const HaloPlan hp = halo_plan(g);
   const int R = g.rad;
-  for (long long u = ((long long)blockIdx.x * kAdjThreads + threadIdx.x) >> 5; u < units; u += nwarps) {
-    const int r = (int)(u / nseg), seg = (int)(u - (long long)r * nseg);
-    int i, j;
-    row_ij(g, r, i, j);
-    int c;
-    if (row_interior(g, i, j)) {
-      if (seg != 0 || lane >= 2 * R) continue;
-      c = lane < R ? lane : g.last - 2 * R + lane;
+  const long long tid = (long long)blockIdx.x * kAdjThreads + threadIdx.x;
+  int i, j = 0, c;
+  if (tid < hp.na) {
+    const long long row = tid / (2 * R);
+    const int e = (int)(tid - row * 2 * R);
+    if (g.dim == 2) {
+      if (row >= g.d0 - 2 * R) return;
+      i = R + (int)row;
     } else {
-      c = seg * 32 + lane;
-      if (c >= g.last) continue;
+      const int w1 = g.d1 - 2 * R;
+      if (row >= (long long)(g.d0 - 2 * R) * w1) return;
+      i = R + (int)(row / w1);
+      j = R + (int)(row - (long long)(i - R) * w1);
     }
-    T acc = T(0);
-    static_for<ST::kTerms>([&](auto TI) {
-      constexpr int t = decltype(TI)::value;
-      constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
-      // 2-D offsets are (row, column); 3-D (plane, row, column)
-      const T l = ST::kDim == 2 ? ldz(lam, g, i - di, 0, c - dj) : ldz(lam, g, i - di, j - dj, c - dk);
-      acc = fma(cf.c[t], l, acc);
-    });
-    const long long o = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift + c;
-    hg[o] += acc;
+    c = e < R ? e : g.last - 2 * R + e;
+  } else {
+    const long long b = tid - hp.na;
+    const long long wrow = (b >> 5) / hp.nseg;
+    const int seg = (int)((b >> 5) - wrow * hp.nseg);
+    if (wrow >= hp.rows_b) return;
+    c = seg * 32 + (int)(b & 31);
+    if (c >= g.last) return;
+    if (g.dim == 2) {
+      i = wrow < R ? (int)wrow : g.d0 - 2 * R + (int)wrow;
+    } else {
+      const long long full = 2LL * R * g.d1;  // rows of the all-halo planes
+      if (wrow < full) {
+        const int p = (int)(wrow / g.d1);
+        i = p < R ? p : g.d0 - 2 * R + p;
+        j = (int)(wrow - (long long)p * g.d1);
+      } else {
+        const long long q = wrow - full;
+        i = R + (int)(q / (2 * R));
+        const int jj = (int)(q - (long long)(i - R) * 2 * R);
+        j = jj < R ? jj : g.d1 - 2 * R + jj;
+      }
+    }
   }
+  T acc = T(0);
+  static_for<ST::kTerms>([&](auto TI) {
+    constexpr int t = decltype(TI)::value;
+    constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
+    // 2-D offsets are (row, column); 3-D (plane, row, column)
+    const T l = ST::kDim == 2 ? ldz(lam, g, i - di, 0, c - dj) : ldz(lam, g, i - di, j - dj, c - dk);
+    acc = fma(cf.c[t], l, acc);
+  });
+  const long long o = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift + c;
+  hg[o] += acc;
 }
 
 // part[blockIdx.x][k] += sum over interior x of lam(x) u(x + o_k) / d.
@@ -414,11 +456,11 @@ struct AdjKernels {
                       double, bool, cudaStream_t);
 };
 
-// one warp per (row, 32-column segment), at most 65536 CTAs (grid-stride beyond)
+// one thread per halo cell of the interior rows, one warp per segment of an all-halo row
 unsigned halo_grid(const AdjGeom &g) {
-  const long long warps = (long long)g.rows * ((g.last + 31) / 32);
-  const long long blocks = (warps * 32 + kAdjThreads - 1) / kAdjThreads;
-  return (unsigned)std::max<long long>(1, std::min<long long>(blocks, 65536));
+  const HaloPlan h = halo_plan(g);
+  const long long threads = h.na + h.rows_b * h.nseg * 32;
+  return (unsigned)std::max<long long>(1, (threads + kAdjThreads - 1) / kAdjThreads);
 }
 
 template <class ST, typename T>
