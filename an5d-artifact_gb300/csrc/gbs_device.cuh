@@ -7,6 +7,16 @@
 #include <type_traits>
 #include <utility>
 
+// Register cap of a build variant (0: none). A kernel of `threads` threads
+// asks for at least 65536 / (threads * cap) resident CTAs per SM, which
+// limits it to about `cap` registers per thread.
+#ifndef GBS_REGCAP
+#define GBS_REGCAP 0
+#endif
+constexpr int gbs_min_ctas(int threads) {
+  return GBS_REGCAP > 0 && 65536 / (threads * GBS_REGCAP) > 1 ? 65536 / (threads * GBS_REGCAP) : 1;
+}
+
 namespace gbs {
 
 // Error bits a kernel ORs into the launch's error word.

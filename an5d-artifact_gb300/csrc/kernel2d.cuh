@@ -413,7 +413,7 @@ __device__ __forceinline__ void warp_ring2d(unsigned char *smem_raw, T *&ring, u
 }
 
 template <class ST, typename T, int B, bool FMA, int WPC, int NSTAGE>
-__global__ void __launch_bounds__(WPC * 32)
+__global__ void __launch_bounds__(WPC * 32, gbs_min_ctas(WPC * 32))
     stencil2d_kernel(const __grid_constant__ Params2D<T, ST::kTerms> p) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const long long gw = (long long)blockIdx.x * WPC + (threadIdx.x >> 5);

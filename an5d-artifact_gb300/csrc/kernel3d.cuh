@@ -145,7 +145,7 @@ struct Smem3 {
 };
 
 template <class ST, typename T, int B, bool FMA, int TJ>
-__global__ void __launch_bounds__(TJ * 32, 1)
+__global__ void __launch_bounds__(TJ * 32, gbs_min_ctas(TJ * 32))
     stencil3d_kernel(const __grid_constant__ Params3D<T, ST::kTerms> p) {
   using SM = Smem3<ST, T, FMA>;
   constexpr int V = SM::V;
@@ -433,7 +433,7 @@ struct Rows3 {
 };
 
 template <class ST, typename T, int B, int NW, int H>
-__global__ void __launch_bounds__(NW * 32, 1)
+__global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
     stencil3d_rows_kernel(const __grid_constant__ Params3D<T, ST::kTerms> p) {
   using G = Rows3<ST, T, B, NW, H>;
   constexpr int V = G::V, R = G::R, W = G::W, ROW = G::ROW, TJ = G::TJ;

@@ -223,6 +223,22 @@ gbs_status gbs_tune_lookup(const gbs_desc *d, int *bt, int *sl) {
   return GBS_OK;
 }
 
+gbs_status gbs_tune_model(const gbs_desc *d, double *ms_per_step) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!ms_per_step) return fail(GBS_ERR_INVALID, "NULL output");
+  gbs_plan_info pi;
+  if ((st = gbs_plan(d, &pi)) != GBS_OK) return st;
+  const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  const Layout L = make_layout(d);
+  double cells = 1.0;
+  for (int a = 0; a < s->dim; ++a) cells *= (double)d->n[a];
+  const double per_cell = std::max(2.0 * (double)L.esize / (pi.bt * hbm_bytes_per_s()),
+                                   pi.redundancy * s->fpp / fp_flops_per_s(d->dtype));
+  *ms_per_step = (cells * per_cell + 3e-6 / pi.bt) * 1e3;
+  return GBS_OK;
+}
+
 gbs_status gbs_tune(const gbs_desc *d, gbs_tune_candidate *cands, int max_cands, int *ncands) {
   gbs_status st = check_desc(d);
   if (st != GBS_OK) return st;

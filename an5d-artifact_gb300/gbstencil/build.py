@@ -6,7 +6,8 @@ values) so that nvcc runs them in parallel. Objects are cached under
 ``_build/`` keyed by a hash of the flags and every source they include, so a
 rebuild only recompiles what changed. No cmake: plain nvcc.
 
-    python -m gbstencil.build          # from an5d-artifact_gb300/
+    python -m gbstencil.build               # from an5d-artifact_gb300/
+    python -m gbstencil.build --regcap=64   # register-capped variant
 """
 from __future__ import annotations
 
@@ -70,10 +71,10 @@ def source_hash(src: Path, flags) -> str:
     return h.hexdigest()
 
 
-def compile_unit(unit, verbose=False):
+def compile_unit(unit, verbose=False, build_dir=BUILD):
     name, src, flags = unit
-    obj = BUILD / f"{name}.o"
-    stamp = BUILD / f"{name}.hash"
+    obj = build_dir / f"{name}.o"
+    stamp = build_dir / f"{name}.hash"
     key = source_hash(src, flags)
     if obj.exists() and stamp.exists() and stamp.read_text() == key:
         return name, False, ""
@@ -85,32 +86,47 @@ def compile_unit(unit, verbose=False):
     return name, True, r.stderr if verbose else ""
 
 
-def build(jobs: int | None = None, verbose: bool = False) -> Path:
-    BUILD.mkdir(exist_ok=True)
-    LIBDIR.mkdir(exist_ok=True)
+def lib_path(regcap: int = 0) -> Path:
+    """The library of a build; regcap > 0: the register-capped variant."""
+    return LIB if regcap <= 0 else LIBDIR / f"regcap{regcap}" / "libgbstencil.so"
+
+
+def build(jobs: int | None = None, verbose: bool = False, regcap: int = 0) -> Path:
+    """Compiles and links the engine. regcap > 0 builds a variant whose
+    stencil kernels are limited to about that many registers per thread
+    (through their launch bounds' minimum resident CTAs per SM), the
+    counterpart of the artifact's REGNUM sweep (all.sh:14-19, nvcc
+    --maxrregcount in make_sconf.sh)."""
+    build_dir = BUILD if regcap <= 0 else BUILD.parent / f"_build_regcap{regcap}"
+    lib = lib_path(regcap)
+    build_dir.mkdir(exist_ok=True)
+    lib.parent.mkdir(parents=True, exist_ok=True)
     jobs = jobs or max(1, os.cpu_count() or 1)
     us = units()
+    if regcap > 0:
+        us = [(n, s, f + [f"-DGBS_REGCAP={regcap}"]) for n, s, f in us]
     # big-radius 3-D boxes first: they are the slowest units
     us.sort(key=lambda u: 0 if "picks_1" in u[0] else 1)
     changed = False
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        for name, did, log in ex.map(lambda u: compile_unit(u, verbose), us):
+        for name, did, log in ex.map(lambda u: compile_unit(u, verbose, build_dir), us):
             changed |= did
             if verbose and log:
                 print(log)
-    if changed or not LIB.exists():
-        objs = [str(BUILD / f"{u[0]}.o") for u in us]
-        tmp = LIB.with_suffix(".so.tmp")
+    if changed or not lib.exists():
+        objs = [str(build_dir / f"{u[0]}.o") for u in us]
+        tmp = lib.with_suffix(".so.tmp")
         cmd = [nvcc(), "-shared"] + ARCH + ["-cudart", "shared", "-o", str(tmp)] + objs + [
             "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
     import time
     t0 = time.time()
-    print(build(verbose="-v" in sys.argv), f"{time.time() - t0:.1f}s")
+    cap = next((int(a.split("=")[1]) for a in sys.argv if a.startswith("--regcap=")), 0)
+    print(build(verbose="-v" in sys.argv, regcap=cap), f"{time.time() - t0:.1f}s")

@@ -9,12 +9,14 @@ from __future__ import annotations
 
 import ctypes
 import json
+import os
 from pathlib import Path
 
 import numpy as np
 
 PKG = Path(__file__).resolve().parent
-LIB_PATH = PKG / "_lib" / "libgbstencil.so"
+# GBS_LIB selects another build of the engine (e.g. a register-capped variant)
+LIB_PATH = Path(os.environ["GBS_LIB"]) if os.environ.get("GBS_LIB") else PKG / "_lib" / "libgbstencil.so"
 TABLE = json.loads((PKG / "stencils.json").read_text())["stencils"]
 NAMES = [s["name"] for s in TABLE]
 
@@ -92,6 +94,7 @@ SIGNATURES = [
     ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gbs_tune", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     ("gbs_tune_set", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    ("gbs_tune_model", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.POINTER(ctypes.c_double)]),
     ("gbs_tune_lookup", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     ("gbs_tune_load", ctypes.c_int, [ctypes.c_char_p]),
     ("gbs_tune_save", ctypes.c_int, [ctypes.c_char_p]),

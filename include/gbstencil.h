@@ -147,6 +147,8 @@ typedef struct gbs_tune_candidate {
 } gbs_tune_candidate;
 gbs_status gbs_tune(const gbs_desc *d, gbs_tune_candidate *cands, int max_cands, int *ncands);
 gbs_status gbs_tune_set(const gbs_desc *d, int bt, int sl, double ms_per_step);
+/* the model's time per step for d as planned (d->bt / d->sl or the table's) */
+gbs_status gbs_tune_model(const gbs_desc *d, double *ms_per_step);
 gbs_status gbs_tune_lookup(const gbs_desc *d, int *bt, int *sl); /* bt = 0: no entry */
 gbs_status gbs_tune_load(const char *path);
 gbs_status gbs_tune_save(const char *path);

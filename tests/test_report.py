@@ -1,0 +1,41 @@
+"""The artifact's result tables (compiled/run.sh, run_sconf.sh) from this engine."""
+import csv
+
+import numpy as np
+import pytest
+
+from gbstencil import capi, report
+
+
+def test_max_degree_matches_plan():
+    # 3-D radius >= 3 kernels are built for one fused step only; 2-D stars to 8 (FMA)
+    assert report.max_degree("star3d3r", np.float32, "fma") == 1
+    assert report.max_degree("star2d1r", np.float32, "fma") == 8
+    assert report.max_degree("j3d27pt", np.float64, "fma") == 2
+
+
+def test_sconf_stencils_are_the_papers_seven():
+    assert report.SCONF_STENCILS == ["j2d5pt", "j2d9pt-gol", "j2d9pt", "gradient2d", "star3d1r", "star3d2r", "j3d27pt"]
+    assert all(n in capi.NAMES for n in report.SCONF_STENCILS)
+
+
+@pytest.mark.gpu
+def test_run_csv_format(tmp_path):
+    report.main(["run", "--prec", "float", "--out", str(tmp_path), "-t", "4", "-n", "1", "--s2", "256",
+                 "--s3", "48", "--stencils", "star2d1r,j3d27pt"])
+    rows = list(csv.reader(open(tmp_path / "float_run.csv")))
+    assert rows[0] == ["Stencil", "bS1", "bS2", "bT", "sl", "Model", "Measured"]
+    assert [r[0] for r in rows[1:]] == ["star2d1r", "j3d27pt"]
+    two, three = rows[1], rows[2]
+    assert two[2] == "" and three[2] != ""          # bS2 only for 3-D, as run.sh writes it
+    for r in rows[1:]:
+        assert int(r[3]) >= 1 and float(r[6]) > 0 and float(r[5].replace(",", "")) > 0
+
+
+@pytest.mark.gpu
+def test_sconf_csv(tmp_path):
+    report.main(["sconf", "--out", str(tmp_path), "-t", "8", "-n", "1", "--s2", "256", "--s3", "48"])
+    rows = list(csv.reader(open(tmp_path / "sconf.csv")))
+    assert len(rows) == 1 + 2 * len(report.SCONF_STENCILS)
+    for r in rows[1:]:
+        assert int(r[4]) <= 4 and float(r[6]) > 0
