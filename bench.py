@@ -83,6 +83,23 @@ def select_work(args):
     return work
 
 
+def rank_specs(count, rank, world, tmax=512):
+    """The batched grids of one rank: rank 0 of a single-GPU run gets the
+    standard seeded set; under N ranks each rank gets its own seeded set of
+    the same size (weak scaling, no data shared between ranks)."""
+    return batched_specs(count, seed=20250101 + (rank if world > 1 else 0), tmax=tmax)
+
+
+def max_over_ranks(ms: float, world: int, device=None) -> float:
+    """The slowest rank's time (all ranks take part; world 1: ms itself)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def batched_specs(count=512, seed=20250101, tmax=512):
     rng = np.random.default_rng(seed)
     out = []
@@ -213,11 +230,7 @@ def run_ours(args, rank, world):
             for gi in range(len(grids)):
                 per_grid_ms[gi] += ev[gi][0].elapsed_time(ev[gi][1])
     capi.sync(stream.cuda_stream)
-    total_ms = sum(per_grid_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(per_grid_ms), world, dev)
     ms_per_step = total_ms / args.steps
     value = cells * world / (ms_per_step * 1e-3) / 1e9
 
@@ -338,7 +351,12 @@ def batched_cpu_work(args, count=16):
 
 
 def cpu_work(args):
-    return batched_cpu_work(args) if args.workload == "batched" else select_work(args)
+    if args.workload == "batched":
+        return batched_cpu_work(args)
+    if args.workload == "adjoint":
+        # the forward loop of each adjoint case (the artifact has no adjoint)
+        return [(name, dt, n[0], T) for name, dt, n, T, *_ in ADJOINT_CASES[:3]]
+    return select_work(args)
 
 
 def run_reference(args, rank, world):
@@ -374,9 +392,7 @@ def run_batched(args, rank, world):
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
-    specs = batched_specs(args.batch_grids, tmax=args.batch_tmax)
-    if world > 1:  # weak scaling: each rank its own grids
-        specs = batched_specs(args.batch_grids, seed=20250101 + rank, tmax=args.batch_tmax)
+    specs = rank_specs(args.batch_grids, rank, world, tmax=args.batch_tmax)
     grids, entries = [], []
     for i, (name, n, T) in enumerate(specs):
         g = DeviceGrid(name, np.float32, n, device=dev)
@@ -406,10 +422,7 @@ def run_batched(args, rank, world):
             torch.cuda.synchronize()
             ms += e0.elapsed_time(e1)
     capi.sync(stream.cuda_stream)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     ms_step = ms / args.steps
     value = cells * world / (ms_step * 1e-3) / 1e9
 
@@ -478,13 +491,144 @@ def run_batched(args, rank, world):
     return line
 
 
+# The adjoint cases: (stencil, dtype, interior, T, checkpoint interval, loss,
+# coefficient gradients wanted)
+ADJOINT_CASES = [
+    ("j2d5pt", np.float32, [2048, 2048], 1024, 32, "half_sq_err", True),
+    ("gradient2d", np.float64, [4096, 4096], 512, 32, "mean_sq", False),
+    ("j3d27pt", np.float32, [384, 384, 384], 256, 16, "half_sq", False),
+] + [("j3d27pt", np.float32, [n, n, n], 256, 16, "half_sq", False)
+     for n in (192, 224, 256, 288, 320, 336, 352, 384)]
+
+
+def run_adjoint(args, rank, world):
+    """Forward with checkpoints + backward (gbs_adjoint_*) per case, against
+    the plain forward loop at the tuned degree."""
+    import torch
+    from gbstencil import capi
+    from gbstencil.adjoint import Checkpointed
+    from gbstencil.grid import DeviceGrid
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    cases, tot_cells, tot_bwd, tot_e2e, h2d, d2h, launches = [], 0, 0.0, 0.0, 0, 0, 0
+    gen = torch.Generator(device=dev)
+    for ci, (name, dt, n, T, C, loss, want_coef) in enumerate(ADJOINT_CASES):
+        tdt = torch.float32 if dt == np.float32 else torch.float64
+        s = capi.info(name)
+        shape = [x + 2 * s["rad"] for x in n]
+        gen.manual_seed(20250101 + ci)
+        u0 = torch.rand(shape, generator=gen, dtype=tdt, device=dev)
+        target = torch.rand(shape, generator=gen, dtype=tdt, device=dev)
+        cells = int(np.prod(n)) * T
+
+        def lam_of(uT):
+            if loss == "half_sq_err":
+                return uT - target          # d/du 0.5 |u - target|^2
+            if loss == "mean_sq":
+                return 2.0 * uT / uT.numel()
+            return uT.clone()               # d/du 0.5 |u|^2
+
+        # plain forward at the tuned degree
+        g = DeviceGrid(name, dt, n, device=dev)
+        g.plane(0).copy_(u0)
+        g.plane(1).copy_(u0)
+        fwd = []
+        for k in range(args.warmup + args.steps):
+            flush.fill_(1.0)
+            e0.record(stream)
+            g.run(T)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                fwd.append(e0.elapsed_time(e1))
+        capi.sync(stream.cuda_stream)
+        plain = capi.plan(g.desc(T)[0])
+        del g
+        run = Checkpointed(name, u0, T, C)
+        lam = lam_of(run.u_T)
+        bwd, ck = [], []
+        for k in range(args.warmup + args.steps):
+            flush.fill_(1.0)
+            e0.record(stream)
+            run = Checkpointed(name, u0, T, C)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ck_ms = e0.elapsed_time(e1)
+            flush.fill_(1.0)
+            e0.record(stream)
+            gu, gc = run.backward(lam, want_coef=want_coef)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                bwd.append(e0.elapsed_time(e1))
+                ck.append(ck_ms)
+        capi.sync(stream.cuda_stream)
+        # end to end: host u_0 in, forward with checkpoints, backward, host gradient out
+        hu0 = u0.cpu().pin_memory()
+        hgrad = torch.empty_like(hu0).pin_memory()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        du0 = hu0.to(dev, non_blocking=True)
+        run = Checkpointed(name, du0, T, C)
+        gu, gc = run.backward(lam_of(run.u_T), want_coef=want_coef)
+        hgrad.copy_(gu, non_blocking=True)
+        torch.cuda.synchronize()
+        tot_e2e += (time.perf_counter() - t0) * 1e3
+        h2d += hu0.numel() * hu0.element_size()
+        d2h += hgrad.numel() * hgrad.element_size()
+        del run
+        torch.cuda.empty_cache()
+        f_ms, b_ms, c_ms = statistics.median(fwd), statistics.median(bwd), statistics.median(ck)
+        per_step = 2 if s["kind"] != "gradient" and not want_coef else (4 if want_coef else 3)
+        launches += (T * per_step + plain.launches) * args.steps
+        tot_cells += cells
+        tot_bwd += b_ms
+        cases.append({"stencil": name, "dtype": np.dtype(dt).name, "n": n, "T": T, "checkpoint_every": C,
+                      "loss": loss, "coef_grad": want_coef, "forward_ms": round(f_ms, 3),
+                      "forward_bt": plain.bt, "forward_checkpointed_ms": round(c_ms, 3),
+                      "backward_ms": round(b_ms, 3), "backward_vs_forward": round(b_ms / f_ms, 3),
+                      "backward_gcells_s": round(cells / (b_ms * 1e-3) / 1e9, 2)})
+    tot_bwd = max_over_ranks(tot_bwd, world, dev)
+    value = tot_cells * world / (tot_bwd * 1e-3) / 1e9
+    hbm, peak_kind = load_peaks()
+    # dominant case (largest backward time): algorithmic bytes per cell step
+    # 2S (linear, dL/du0 only), 6S (with coefficients), 10S (gradient2d:
+    # recompute 2S, pre-pass 3S, gather 5S)
+    dom = max(cases, key=lambda c: c["backward_ms"])
+    S = np.dtype(dom["dtype"]).itemsize
+    per_cell = 10 * S if dom["stencil"] == "gradient2d" else (6 * S if dom["coef_grad"] else 2 * S)
+    dcells = int(np.prod(dom["n"])) * dom["T"]
+    achieved = per_cell * dcells / (dom["backward_ms"] * 1e-3) / 1e9
+    return {
+        "metric": METRIC, "value": round(value, 3), "unit": "GCells/s (backward cell-steps)", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot_bwd, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic U[0,1) initial grids and targets, seeded",
+        "config": {"workload": "adjoint", "cases": [f"{c['stencil']} {c['dtype']} {'x'.join(map(str, c['n']))} "
+                                                     f"T={c['T']} C={c['checkpoint_every']}" for c in cases],
+                   "l2": "flushed between timed runs (512 MB write)", "parallelism": "replicas" if world > 1 else "single GPU"},
+        "adjoint": cases,
+        "e2e": {"value": round(tot_cells / (tot_e2e * 1e-3) / 1e9, 3), "unit": "GCells/s (forward+backward, host buffers)",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "kernel": f"backward of {dom['stencil']} {dom['dtype']} {'x'.join(map(str, dom['n']))}",
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "gpu_launches": launches,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="suite3d", choices=sorted(WORKLOADS) + ["batched"])
+    ap.add_argument("--workload", default="suite3d", choices=sorted(WORKLOADS) + ["batched", "adjoint"])
     ap.add_argument("--fp-mode", default="fma", choices=["fma", "exact"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
@@ -506,7 +650,12 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    line = run_batched(args, rank, world) if args.workload == "batched" else run_ours(args, rank, world)
+    if args.workload == "batched":
+        line = run_batched(args, rank, world)
+    elif args.workload == "adjoint":
+        line = run_adjoint(args, rank, world)
+    else:
+        line = run_ours(args, rank, world)
     if rank == 0:
         if not args.no_cpu:
             import pyoracle as po
