@@ -609,16 +609,125 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_run_noalloc)(const gbs_batch_grid
 extern "C++" gbs_status gbs_batch_build_0(const gbs_batch_grid *, int, int, gbs_batch **);
 extern "C++" gbs_status gbs_batch_run_noalloc_0(const gbs_batch_grid *, int, cudaStream_t);
 
+namespace gbs {
+namespace {
+// GBS_BATCH_STREAMS: each grid's own time loop (the engine's plain kernels at
+// the tuned degree) captured as a chain of kernel nodes; the chains are
+// spread over kStreams capture streams, heaviest first onto the least loaded
+// one, so independent grids run side by side. One graph launch.
+constexpr int kStreams = 16;
+
+gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, gbs_batch **out) {
+  if (!grids || ngrids <= 0) return fail(GBS_ERR_INVALID, "batch: no grids");
+  std::vector<gbs_desc> ds(ngrids);
+  std::vector<double> work(ngrids);
+  long long cells = 0;
+  int launches = 0;
+  for (int g = 0; g < ngrids; ++g) {
+    const gbs_batch_grid &bg = grids[g];
+    const gbs_stencil_def_t *s = stencil_def(bg.stencil);
+    if (!s || s->dim != 2) return fail(GBS_ERR_INVALID, "batch grid %d: not a 2-D stencil", g);
+    if (bg.n[0] < 1 || bg.n[1] < 1 || bg.timestep < 0 || !bg.dev_A)
+      return fail(GBS_ERR_INVALID, "batch grid %d: bad extent, timestep or buffer", g);
+    if (reinterpret_cast<uintptr_t>(bg.dev_A) % 128 != 0)
+      return fail(GBS_ERR_INVALID, "batch grid %d: buffer not 128-byte aligned", g);
+    gbs_desc &d = ds[g];
+    d = gbs_desc{};
+    d.stencil = bg.stencil;
+    d.dtype = GBS_F32;
+    d.n[0] = bg.n[0];
+    d.n[1] = bg.n[1];
+    d.n[2] = 1;
+    d.timestep = bg.timestep;
+    d.fp_mode = fp_mode;
+    d.coef = bg.coef;
+    d.divisor = bg.divisor;
+    gbs_status st = check_desc(&d);
+    if (st != GBS_OK) return st;
+    gbs_plan_info pi;
+    if ((st = gbs_plan(&d, &pi)) != GBS_OK) return st;
+    launches += pi.launches;
+    cells += (long long)bg.n[0] * bg.n[1] * bg.timestep;
+    work[g] = (double)bg.n[0] * bg.n[1] * bg.timestep;
+  }
+  int *err = nullptr;
+  gbs_status st = error_word(&err);
+  if (st != GBS_OK) return st;
+  std::vector<int> order(ngrids);
+  for (int g = 0; g < ngrids; ++g) order[g] = g;
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+  auto *h = new gbs_batch();
+  h->ngrids = ngrids;
+  h->cells = cells;
+  h->launches_plain = launches;
+  h->mode = GBS_BATCH_STREAMS;
+  cudaStream_t cs = nullptr, side[kStreams] = {};
+  cudaEvent_t fork = nullptr, join[kStreams] = {};
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  for (int k = 0; k < kStreams && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  for (int k = 0; k < kStreams && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming);
+  auto release = [&]() {
+    for (int k = 0; k < kStreams; ++k) {
+      if (join[k]) cudaEventDestroy(join[k]);
+      if (side[k]) cudaStreamDestroy(side[k]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    if (cs) cudaStreamDestroy(cs);
+  };
+  if (e != cudaSuccess) {
+    release();
+    delete h;
+    return cuda_fail(e, "batch: streams");
+  }
+  st = GBS_OK;
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaEventRecord(fork, cs);
+    for (int k = 0; k < kStreams; ++k) cudaStreamWaitEvent(side[k], fork, 0);
+    double load[kStreams] = {};
+    for (int g : order) {
+      const int k = (int)(std::min_element(load, load + kStreams) - load);
+      load[k] += work[g];
+      const Layout L = make_layout(&ds[g]);
+      st = run_loop(&ds[g], L, grids[g].dev_A, side[k], err);
+      if (st != GBS_OK) break;
+    }
+    for (int k = 0; k < kStreams; ++k) {
+      cudaEventRecord(join[k], side[k]);
+      cudaStreamWaitEvent(cs, join[k], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(cs, &graph);
+    h->graph = graph;
+  }
+  if (st == GBS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&h->exec, h->graph, 0);
+  release();
+  if (st != GBS_OK || e != cudaSuccess) {
+    gbs_batch_destroy(h);
+    return st != GBS_OK ? st : cuda_fail(e, "batch: graph capture");
+  }
+  h->kernels = launches;
+  h->nitems = launches;
+  *out = h;
+  return GBS_OK;
+}
+}  // namespace
+}  // namespace gbs
+
 extern "C" {
 gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, int mode,
                           gbs_batch **out) {
-  if (mode != GBS_BATCH_PERSISTENT && mode != GBS_BATCH_LAYERED) return fail(GBS_ERR_INVALID, "bad batch mode");
+  if (mode != GBS_BATCH_PERSISTENT && mode != GBS_BATCH_LAYERED && mode != GBS_BATCH_STREAMS)
+    return fail(GBS_ERR_INVALID, "bad batch mode");
   if (dtype != GBS_F32) return fail(GBS_ERR_UNSUPPORTED, "batched launch supports GBS_F32 grids");
   if (fp_mode != GBS_FP_EXACT && fp_mode != GBS_FP_FMA) return fail(GBS_ERR_INVALID, "bad fp_mode");
   if (!out) return fail(GBS_ERR_INVALID, "out is NULL");
   gbs_batch *h = nullptr;
-  gbs_status st = fp_mode == GBS_FP_FMA ? gbs_batch_build_1(grids, ngrids, mode, &h)
-                                        : gbs_batch_build_0(grids, ngrids, mode, &h);
+  gbs_status st;
+  if (mode == GBS_BATCH_STREAMS) st = build_streams(grids, ngrids, fp_mode, &h);
+  else st = fp_mode == GBS_FP_FMA ? gbs_batch_build_1(grids, ngrids, mode, &h)
+                                  : gbs_batch_build_0(grids, ngrids, mode, &h);
   *out = h;
   return st;
 }

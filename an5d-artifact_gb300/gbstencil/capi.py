@@ -217,7 +217,7 @@ def sync(stream: int = 0):
 class Batch:
     """A planned batched launch (gbs_batch_plan) over device grids."""
 
-    MODES = {"persistent": 0, "layered": 1}
+    MODES = {"persistent": 0, "layered": 1, "streams": 2}
 
     def __init__(self, grids, fp_mode="fma", mode="persistent"):
         """grids: list of (DeviceGrid-like with .name, .n, .buf, timestep, coef or None)."""

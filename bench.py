@@ -637,7 +637,7 @@ def main():
     ap.add_argument("--T", type=int, default=0, help="timestep override")
     ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
-    ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "layered"],
+    ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "layered", "streams"],
                     help="batched workload: scheduling of the work items")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

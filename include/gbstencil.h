@@ -185,7 +185,7 @@ typedef struct gbs_batch_stats {
   int plain_launches;      /* kernel launches the same work takes one grid at a time */
   long long cell_updates;  /* sum of n[0]*n[1]*timestep */
   int kernels;             /* kernel nodes in the plan's graph */
-  int mode;                /* GBS_BATCH_PERSISTENT | GBS_BATCH_LAYERED */
+  int mode;                /* GBS_BATCH_PERSISTENT | GBS_BATCH_LAYERED | GBS_BATCH_STREAMS */
 } gbs_batch_stats;
 
 /* How a batch plan schedules its work items (grid, time block, strip,
@@ -195,8 +195,12 @@ typedef struct gbs_batch_stats {
  *   counters for the grid's previous time block.
  * GBS_BATCH_LAYERED: one kernel node per time block in the graph, each over
  *   every grid's items of that block; kernel boundaries order the blocks, so
- *   nothing waits on the device. */
-enum { GBS_BATCH_PERSISTENT = 0, GBS_BATCH_LAYERED = 1 };
+ *   nothing waits on the device.
+ * GBS_BATCH_STREAMS: each grid's own time loop (the single-grid kernels at
+ *   the tuned degree, one kernel node per fused launch) as a chain in the
+ *   graph; the chains are spread over 16 branches, heaviest grid first onto
+ *   the least loaded branch, so independent grids run side by side. */
+enum { GBS_BATCH_PERSISTENT = 0, GBS_BATCH_LAYERED = 1, GBS_BATCH_STREAMS = 2 };
 
 /* Plans the batch: work items, per-grid dependency counters and the CUDA
  * graph (counter reset + the persistent kernel). Allocates device memory

@@ -26,7 +26,7 @@ def make_batch(seed, count, nmax, tmax):
     return specs
 
 
-@pytest.mark.parametrize("sched", ["persistent", "layered"])
+@pytest.mark.parametrize("sched", ["persistent", "layered", "streams"])
 @pytest.mark.parametrize("mode", ["exact", "fma"])
 def test_batch_matches_oracle(mode, sched):
     specs = make_batch(7, 40, 300, 23)
