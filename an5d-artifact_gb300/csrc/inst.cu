@@ -39,6 +39,7 @@ constexpr int tile_rows_b(int b) { return rows_pick(b, std::make_integer_sequenc
 // lower; it keeps degrees up to 4. In 3-D a tile of 32 rows loses 2*b*r rows
 // to overlap, and FP64 is compute-bound from b=1.
 constexpr int max_class() {
+  if (!kFma && !S::kExact) return 0;  // no exact form (3d125pt: float group sums combined in double)
   if (S::kDim == 2) {
     if (sizeof(T) == 8) return 2;
     if (S::kKind == KIND_GRADIENT) return 2;  // FP64 root and quotient

@@ -20,7 +20,12 @@ Nothing here is hand-entered: the coefficients, the term order (which fixes
 the floating-point summation order) and the quirks (the doubled
 ``A[i-4][j]`` tap of ``star2d4r.c:19,24``, the ``/118`` and ``/159``
 divisors, the nonlinear ``gradient2d.c:17-21``) all come from the source.
-``3d125pt.c`` is not part of the artifact's benchmark set and is skipped.
+``3d125pt.c`` (not in the artifact's benchmark set) has a third form: a sum
+of groups ``c * (A + A + ...)`` with double literals, whose float build
+sums each group in float and combines the groups in double. Its record
+lists the groups and its terms (one per occurrence, duplicates kept), and it
+has no exact mode in the engine (``exact: false``): the kernel family
+evaluates it in FMA mode only.
 """
 from __future__ import annotations
 
@@ -37,7 +42,7 @@ STENCILS = [
     "j2d5pt", "j2d9pt", "j2d9pt-gol", "gradient2d",
     "star3d1r", "star3d2r", "star3d3r", "star3d4r",
     "box3d1r", "box3d2r", "box3d3r", "box3d4r",
-    "j3d27pt",
+    "j3d27pt", "3d125pt",
 ]
 
 
@@ -113,8 +118,8 @@ class Parser:
     """expr := term (('+'|'-') term)* ; term := unary (('*'|'/') unary)* ;
     unary := '-' unary | atom ; atom := num | ref | id '(' expr ')' | '(' expr ')'"""
 
-    def __init__(self, toks, dim):
-        self.t, self.i, self.dim = toks, 0, dim
+    def __init__(self, toks, names):
+        self.t, self.i, self.names = toks, 0, names
 
     def peek(self):
         return self.t[self.i] if self.i < len(self.t) else (None, None)
@@ -152,8 +157,7 @@ class Parser:
             return ("num", val)
         if kind == "ref":
             idx = re.findall(r"\[([^\]]*)\]", val)[1:]
-            names = ["i", "j", "k"][: self.dim]
-            return ("ref", tuple(parse_index(e, n) for e, n in zip(idx, names)))
+            return ("ref", tuple(parse_index(e, n) for e, n in zip(idx, self.names)))
         if kind == "id":
             self.take("(")
             arg = self.expr()
@@ -215,9 +219,12 @@ def analyse(name: str, src: str):
     scop_start = head.count("\n") + 1
     scop = src.split("#pragma scop", 1)[1].split("#pragma endscop", 1)[0]
     scop_end = scop_start + scop.count("\n")
-    lhs = "A[(t+1)%2]" + "".join(f"[{v}]" for v in "ijk"[:dim]) + " ="
-    rhs = scop.split(lhs, 1)[1].rsplit(";", 1)[0]
-    tree = Parser(tokenize(rhs), dim).expr()
+    # the loop variables in array order, as the assignment indexes A
+    m = re.search(r"A\[\(t\+1\)%2\]((?:\[\w+\])+)\s*=", scop)
+    names = re.findall(r"\[(\w+)\]", m.group(1))
+    assert len(names) == dim, (name, names)
+    rhs = scop[m.end():].rsplit(";", 1)[0]
+    tree = Parser(tokenize(rhs), names).expr()
 
     rec = {"name": name, "dim": dim, "rad": rad, "fpp": fpp,
            "source": f"{name}.c:{scop_start}-{scop_end}"}
@@ -228,20 +235,50 @@ def analyse(name: str, src: str):
         if is_f:
             raise ValueError("float divisor not expected")
         divisor, body = dv, tree[1]
+    rec["exact"] = True
     try:
         terms = linear_terms(body)
         rec.update(kind="linear", terms=terms, divisor=divisor)
     except ValueError:
-        rec.update(analyse_gradient(tree, dim))
+        try:
+            groups = group_terms(body)
+            terms = [{"off": list(o), "literal": g["literal"], "value": g["value"], "group": gi}
+                     for gi, g in enumerate(groups) for o in g["refs"]]
+            rec.update(kind="linear", terms=terms, divisor=divisor, groups=groups, exact=False)
+        except ValueError:
+            rec.update(analyse_gradient(tree, dim))
     if rec["kind"] == "linear":
         rows = [t["off"][0] for t in rec["terms"]]
         rec["grouped"] = all(a <= b for a, b in zip(rows, rows[1:]))
-        rec["form"] = "assoc" if (rec["grouped"] and is_box(rec)) else "direct"
+        if not rec["exact"]:
+            rec["form"] = "assoc"   # FMA mode only: any term order
+        else:
+            rec["form"] = "assoc" if (rec["grouped"] and is_box(rec)) else "direct"
         rec["ntaps"] = len({tuple(t["off"]) for t in rec["terms"]})
         rec["nterms"] = len(rec["terms"])
         rmax = max(max(abs(o) for o in t["off"]) for t in rec["terms"])
         assert rmax == rad, (name, rmax, rad)
     return rec
+
+
+def group_terms(node):
+    """``c1 * (A + A + ...) + c2 * (...) + ...`` with double literals c
+    (3d125pt.c:18-48): [{literal, value, refs: [offset, ...]}] in source
+    order."""
+    groups = []
+    for sgn, t in flatten_sum(node):
+        if sgn < 0 or t[0] != "mul" or t[1][0] != "num":
+            raise ValueError("not a grouped sum")
+        is_f, v = literal_value(t[1][1])
+        if is_f:
+            raise ValueError("grouped sums take double literals")
+        refs = []
+        for s2, r in flatten_sum(t[2]):
+            if s2 < 0 or r[0] != "ref":
+                raise ValueError("group is not a sum of grid references")
+            refs.append(list(r[1]))
+        groups.append({"literal": t[1][1], "value": float(v), "refs": refs})
+    return groups
 
 
 def is_box(rec):
@@ -310,6 +347,7 @@ def emit_header(recs) -> str:
         out.append(f"  static constexpr bool kHasDiv = {'true' if r['divisor'] else 'false'};")
         out.append(f"  static constexpr bool kGrouped = {'true' if r['grouped'] else 'false'};")
         out.append(f"  static constexpr bool kAssoc = {'true' if r['form'] == 'assoc' else 'false'};")
+        out.append(f"  static constexpr bool kExact = {'true' if r.get('exact', True) else 'false'};")
         offs_all = [t["off"] for t in r["terms"]] if r["kind"] == "linear" else r["neighbours"]
         rows = ", ".join("{" + ", ".join(str(v) for v in (list(o) + [0] * (3 - len(o)))) + "}" for o in offs_all)
         out.append(f"  static constexpr int kOff[kTerms][3] = {{{rows}}};")
@@ -344,7 +382,7 @@ def emit_host_table(recs) -> str:
     out = [
         "// Generated by gbstencil/gen_stencil_table.py. Do not edit by hand.",
         "#pragma once",
-        "typedef struct { int di, dj, dk; float coef; } gbs_tap_t;",
+        "typedef struct { int di, dj, dk; double coef; } gbs_tap_t;",
         "typedef struct {",
         "  const char *name; int dim, rad, fpp, kind, nterms, grouped, assoc;",
         "  int divisor;            /* 0 = none */",
@@ -359,11 +397,11 @@ def emit_host_table(recs) -> str:
         if r["kind"] == "linear":
             for t in r["terms"]:
                 o = list(t["off"]) + [0] * (3 - r["dim"])
-                out.append(f"  {{{o[0]}, {o[1]}, {o[2]}, {hexf(t['value'])}f}},  /* {t['literal']} */")
+                out.append(f"  {{{o[0]}, {o[1]}, {o[2]}, {hexf(t['value'])}}},  /* {t['literal']} */")
         else:
             for o in r["neighbours"]:
                 o = list(o) + [0] * (3 - r["dim"])
-                out.append(f"  {{{o[0]}, {o[1]}, {o[2]}, 0.0f}},")
+                out.append(f"  {{{o[0]}, {o[1]}, {o[2]}, 0.0}},")
         out.append("};")
     out.append("")
     out.append("static const gbs_stencil_def_t gbs_stencil_defs[] = {")

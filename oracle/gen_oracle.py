@@ -18,7 +18,8 @@ the divisor. ``n`` holds the interior extent per axis (the reference is cubic,
 ``n[0]==n[1]==n[2]==compsize``; the batched tests use uneven grids). The
 gradient form restates ``gradient2d.c:17-21`` with the same C type
 promotions (float squares summed in float, then the double ``sqrt`` and
-division). Compile with ``-ffp-contract=off`` so that no product is fused
+division); the grouped form of ``3d125pt.c:18-48`` sums each group in T and
+combines the groups with their double literals in double. Compile with ``-ffp-contract=off`` so that no product is fused
 into an add: this makes the build's results independent of the host ISA
 (gcc contracts to FMA by default on aarch64, not on x86-64 without -mfma).
 
@@ -75,6 +76,44 @@ def emit_linear(rec, t, T):
     return "\n".join(lines)
 
 
+def emit_grouped(rec, t, T):
+    """3d125pt.c:18-48: sum over groups of ``c * (A + A + ...)`` with double
+    literals c: each group sum in T (left to right), the products and their
+    sum in double (long double for the long double oracle), rounded once on
+    store. coef == NULL: the source literals; else group g takes coef[first
+    term of g] (callers pass group-constant coefficients)."""
+    dim, r = rec["dim"], rec["rad"]
+    name = ident(rec["name"])
+    wide = "long double" if t == "q" else "double"
+    idx = ["i", "j", "k"][:dim]
+    lines = [f"void oracle_{name}_{t}({T} *A1, const int *n, int timestep,",
+             f"    const {T} *coef, {T} divisor, {T} eps)",
+             "{",
+             "  (void)eps; (void)divisor;",
+             f"  const long d0 = n[0] + {2 * r}, d1 = n[1] + {2 * r}, d2 = n[2] + {2 * r};",
+             f"  {T} (*A)[d0][d1][d2] = ({T} (*)[d0][d1][d2])A1;"]
+    first = 0
+    for g, grp in enumerate(rec["groups"]):
+        lines.append(f"  const {wide} c{g} = coef ? ({wide})coef[{first}] : ({wide}){grp['literal']};")
+        first += len(grp["refs"])
+    groups = []
+    for g, grp in enumerate(rec["groups"]):
+        refs = []
+        for off in grp["refs"]:
+            refs.append("A[t%2]" + "".join(f"[{v}{o:+d}]" if o else f"[{v}]" for v, o in zip(idx, off)))
+        groups.append(f"c{g} * ({T})(" + " + ".join(refs) + ")")
+    lhs = "A[(t+1)%2]" + "".join(f"[{v}]" for v in idx)
+    lines += ["  for (int t = 0; t < timestep; t++) {",
+              "#pragma omp parallel for schedule(static)",
+              f"    for (long i = {r}; i < d0 - {r}; i++)",
+              f"      for (long j = {r}; j < d1 - {r}; j++)",
+              f"        for (long k = {r}; k < d2 - {r}; k++)",
+              f"          {lhs} = ({T})(" + "\n            + ".join(groups).replace("\\n", "\n") + ");",
+              "  }",
+              "}"]
+    return "\n".join(lines)
+
+
 def emit_gradient(rec, t, T):
     r = rec["rad"]
     name = ident(rec["name"])
@@ -122,7 +161,9 @@ def main(argv):
     ]
     for rec in recs:
         for t, T in TYPES.items():
-            if rec["kind"] == "linear":
+            if rec["kind"] == "linear" and rec.get("groups"):
+                parts.append(emit_grouped(rec, t, T))
+            elif rec["kind"] == "linear":
                 parts.append(emit_linear(rec, t, T))
             else:
                 parts.append(emit_gradient(rec, t, T))

@@ -5568,6 +5568,90 @@ void oracle_j3d27pt_q(long double *A1, const int *n, int timestep,
   }
 }
 
+void oracle_3d125pt_f(float *A1, const int *n, int timestep,
+    const float *coef, float divisor, float eps)
+{
+  (void)eps; (void)divisor;
+  const long d0 = n[0] + 4, d1 = n[1] + 4, d2 = n[2] + 4;
+  float (*A)[d0][d1][d2] = (float (*)[d0][d1][d2])A1;
+  const double c0 = coef ? (double)coef[0] : (double)0.75;
+  const double c1 = coef ? (double)coef[16] : (double)0.76;
+  const double c2 = coef ? (double)coef[20] : (double)1.132;
+  const double c3 = coef ? (double)coef[50] : (double)0.217;
+  const double c4 = coef ? (double)coef[70] : (double)2.13;
+  const double c5 = coef ? (double)coef[95] : (double)0.331;
+  const double c6 = coef ? (double)coef[121] : (double)0.332;
+  for (int t = 0; t < timestep; t++) {
+#pragma omp parallel for schedule(static)
+    for (long i = 2; i < d0 - 2; i++)
+      for (long j = 2; j < d1 - 2; j++)
+        for (long k = 2; k < d2 - 2; k++)
+          A[(t+1)%2][i][j][k] = (float)(c0 * (float)(A[t%2][i-2][j-2][k-2] + A[t%2][i-2][j-2][k+2] + A[t%2][i-2][j+2][k-2] + A[t%2][i-2][j+2][k+2] + A[t%2][i-1][j-1][k-1] + A[t%2][i-1][j-1][k+1] + A[t%2][i-1][j+1][k-1] + A[t%2][i-1][j+1][k+1] + A[t%2][i][j-1][k] + A[t%2][i][j][k-1] + A[t%2][i][j][k+1] + A[t%2][i][j+1][k] + A[t%2][i+1][j-1][k-1] + A[t%2][i+1][j-1][k+1] + A[t%2][i+1][j+1][k-1] + A[t%2][i+1][j+1][k+1])
+            + c1 * (float)(A[t%2][i-2][j-2][k-2] + A[t%2][i-2][j-2][k+2] + A[t%2][i-2][j+2][k-2] + A[t%2][i-2][j+2][k+2])
+            + c2 * (float)(A[t%2][i-2][j-2][k-1] + A[t%2][i-2][j-2][k+1] + A[t%2][i-2][j-1][k-2] + A[t%2][i-2][j-1][k+2] + A[t%2][i-2][j][k] + A[t%2][i-2][j+1][k-2] + A[t%2][i-2][j+1][k+2] + A[t%2][i-2][j+2][k-1] + A[t%2][i-2][j+2][k+1] + A[t%2][i-1][j-2][k-2] + A[t%2][i-1][j-2][k+2] + A[t%2][i-1][j+2][k-2] + A[t%2][i-1][j+2][k+2] + A[t%2][i][j-2][k] + A[t%2][i][j][k-2] + A[t%2][i][j][k+2] + A[t%2][i][j+2][k] + A[t%2][i+1][j-2][k-2] + A[t%2][i+1][j-2][k+2] + A[t%2][i+1][j+2][k-2] + A[t%2][i+1][j+2][k+2] + A[t%2][i-2][j-2][k-1] + A[t%2][i-2][j-2][k+1] + A[t%2][i-2][j-1][k-2] + A[t%2][i-2][j-1][k+2] + A[t%2][i-2][j][k] + A[t%2][i-2][j+1][k-2] + A[t%2][i-2][j+1][k+2] + A[t%2][i-2][j+2][k-1] + A[t%2][i-2][j+2][k+1])
+            + c3 * (float)(A[t%2][i-2][j-2][k] + A[t%2][i-2][j][k-2] + A[t%2][i-2][j][k+2] + A[t%2][i-2][j+2][k] + A[t%2][i-1][j-1][k] + A[t%2][i-1][j][k-1] + A[t%2][i-1][j][k+1] + A[t%2][i-1][j+1][k] + A[t%2][i][j-2][k-2] + A[t%2][i][j-2][k+2] + A[t%2][i][j+2][k-2] + A[t%2][i][j+2][k+2] + A[t%2][i+1][j-1][k] + A[t%2][i+1][j][k-1] + A[t%2][i+1][j][k+1] + A[t%2][i+1][j+1][k] + A[t%2][i-2][j-2][k] + A[t%2][i-2][j][k-2] + A[t%2][i-2][j][k+2] + A[t%2][i-2][j+2][k])
+            + c4 * (float)(A[t%2][i-2][j-1][k] + A[t%2][i-2][j][k-1] + A[t%2][i-2][j][k+1] + A[t%2][i-2][j+1][k] + A[t%2][i-1][j-2][k] + A[t%2][i-1][j][k-2] + A[t%2][i-1][j][k+2] + A[t%2][i-1][j+2][k] + A[t%2][i][j-2][k-1] + A[t%2][i][j-2][k+1] + A[t%2][i][j-1][k-2] + A[t%2][i][j-1][k+2] + A[t%2][i][j][k] + A[t%2][i][j+1][k-2] + A[t%2][i][j+1][k+2] + A[t%2][i][j+2][k-1] + A[t%2][i][j+2][k+1] + A[t%2][i+1][j-2][k] + A[t%2][i+1][j][k-2] + A[t%2][i+1][j][k+2] + A[t%2][i+1][j+2][k] + A[t%2][i-2][j-1][k] + A[t%2][i-2][j][k-1] + A[t%2][i-2][j][k+1] + A[t%2][i-2][j+1][k])
+            + c5 * (float)(A[t%2][i-2][j-1][k-1] + A[t%2][i-2][j-1][k+1] + A[t%2][i-2][j+1][k-1] + A[t%2][i-2][j+1][k+1] + A[t%2][i-1][j-2][k-1] + A[t%2][i-1][j-2][k+1] + A[t%2][i-1][j-1][k-2] + A[t%2][i-1][j-1][k+2] + A[t%2][i-1][j][k] + A[t%2][i-1][j+1][k-2] + A[t%2][i-1][j+1][k+2] + A[t%2][i-1][j+2][k-1] + A[t%2][i-1][j+2][k+1] + A[t%2][i][j-1][k-1] + A[t%2][i][j-1][k+1] + A[t%2][i][j+1][k-1] + A[t%2][i][j+1][k+1] + A[t%2][i+1][j-2][k-1] + A[t%2][i+1][j-2][k+1] + A[t%2][i+1][j-1][k-2] + A[t%2][i+1][j-1][k+2] + A[t%2][i+1][j][k] + A[t%2][i+1][j+1][k-2] + A[t%2][i+1][j+1][k+2] + A[t%2][i+1][j+2][k-1] + A[t%2][i+1][j+2][k+1])
+            + c6 * (float)(A[t%2][i-2][j-1][k-1] + A[t%2][i-2][j-1][k+1] + A[t%2][i-2][j+1][k-1] + A[t%2][i-2][j+1][k+1]));
+  }
+}
+
+void oracle_3d125pt_d(double *A1, const int *n, int timestep,
+    const double *coef, double divisor, double eps)
+{
+  (void)eps; (void)divisor;
+  const long d0 = n[0] + 4, d1 = n[1] + 4, d2 = n[2] + 4;
+  double (*A)[d0][d1][d2] = (double (*)[d0][d1][d2])A1;
+  const double c0 = coef ? (double)coef[0] : (double)0.75;
+  const double c1 = coef ? (double)coef[16] : (double)0.76;
+  const double c2 = coef ? (double)coef[20] : (double)1.132;
+  const double c3 = coef ? (double)coef[50] : (double)0.217;
+  const double c4 = coef ? (double)coef[70] : (double)2.13;
+  const double c5 = coef ? (double)coef[95] : (double)0.331;
+  const double c6 = coef ? (double)coef[121] : (double)0.332;
+  for (int t = 0; t < timestep; t++) {
+#pragma omp parallel for schedule(static)
+    for (long i = 2; i < d0 - 2; i++)
+      for (long j = 2; j < d1 - 2; j++)
+        for (long k = 2; k < d2 - 2; k++)
+          A[(t+1)%2][i][j][k] = (double)(c0 * (double)(A[t%2][i-2][j-2][k-2] + A[t%2][i-2][j-2][k+2] + A[t%2][i-2][j+2][k-2] + A[t%2][i-2][j+2][k+2] + A[t%2][i-1][j-1][k-1] + A[t%2][i-1][j-1][k+1] + A[t%2][i-1][j+1][k-1] + A[t%2][i-1][j+1][k+1] + A[t%2][i][j-1][k] + A[t%2][i][j][k-1] + A[t%2][i][j][k+1] + A[t%2][i][j+1][k] + A[t%2][i+1][j-1][k-1] + A[t%2][i+1][j-1][k+1] + A[t%2][i+1][j+1][k-1] + A[t%2][i+1][j+1][k+1])
+            + c1 * (double)(A[t%2][i-2][j-2][k-2] + A[t%2][i-2][j-2][k+2] + A[t%2][i-2][j+2][k-2] + A[t%2][i-2][j+2][k+2])
+            + c2 * (double)(A[t%2][i-2][j-2][k-1] + A[t%2][i-2][j-2][k+1] + A[t%2][i-2][j-1][k-2] + A[t%2][i-2][j-1][k+2] + A[t%2][i-2][j][k] + A[t%2][i-2][j+1][k-2] + A[t%2][i-2][j+1][k+2] + A[t%2][i-2][j+2][k-1] + A[t%2][i-2][j+2][k+1] + A[t%2][i-1][j-2][k-2] + A[t%2][i-1][j-2][k+2] + A[t%2][i-1][j+2][k-2] + A[t%2][i-1][j+2][k+2] + A[t%2][i][j-2][k] + A[t%2][i][j][k-2] + A[t%2][i][j][k+2] + A[t%2][i][j+2][k] + A[t%2][i+1][j-2][k-2] + A[t%2][i+1][j-2][k+2] + A[t%2][i+1][j+2][k-2] + A[t%2][i+1][j+2][k+2] + A[t%2][i-2][j-2][k-1] + A[t%2][i-2][j-2][k+1] + A[t%2][i-2][j-1][k-2] + A[t%2][i-2][j-1][k+2] + A[t%2][i-2][j][k] + A[t%2][i-2][j+1][k-2] + A[t%2][i-2][j+1][k+2] + A[t%2][i-2][j+2][k-1] + A[t%2][i-2][j+2][k+1])
+            + c3 * (double)(A[t%2][i-2][j-2][k] + A[t%2][i-2][j][k-2] + A[t%2][i-2][j][k+2] + A[t%2][i-2][j+2][k] + A[t%2][i-1][j-1][k] + A[t%2][i-1][j][k-1] + A[t%2][i-1][j][k+1] + A[t%2][i-1][j+1][k] + A[t%2][i][j-2][k-2] + A[t%2][i][j-2][k+2] + A[t%2][i][j+2][k-2] + A[t%2][i][j+2][k+2] + A[t%2][i+1][j-1][k] + A[t%2][i+1][j][k-1] + A[t%2][i+1][j][k+1] + A[t%2][i+1][j+1][k] + A[t%2][i-2][j-2][k] + A[t%2][i-2][j][k-2] + A[t%2][i-2][j][k+2] + A[t%2][i-2][j+2][k])
+            + c4 * (double)(A[t%2][i-2][j-1][k] + A[t%2][i-2][j][k-1] + A[t%2][i-2][j][k+1] + A[t%2][i-2][j+1][k] + A[t%2][i-1][j-2][k] + A[t%2][i-1][j][k-2] + A[t%2][i-1][j][k+2] + A[t%2][i-1][j+2][k] + A[t%2][i][j-2][k-1] + A[t%2][i][j-2][k+1] + A[t%2][i][j-1][k-2] + A[t%2][i][j-1][k+2] + A[t%2][i][j][k] + A[t%2][i][j+1][k-2] + A[t%2][i][j+1][k+2] + A[t%2][i][j+2][k-1] + A[t%2][i][j+2][k+1] + A[t%2][i+1][j-2][k] + A[t%2][i+1][j][k-2] + A[t%2][i+1][j][k+2] + A[t%2][i+1][j+2][k] + A[t%2][i-2][j-1][k] + A[t%2][i-2][j][k-1] + A[t%2][i-2][j][k+1] + A[t%2][i-2][j+1][k])
+            + c5 * (double)(A[t%2][i-2][j-1][k-1] + A[t%2][i-2][j-1][k+1] + A[t%2][i-2][j+1][k-1] + A[t%2][i-2][j+1][k+1] + A[t%2][i-1][j-2][k-1] + A[t%2][i-1][j-2][k+1] + A[t%2][i-1][j-1][k-2] + A[t%2][i-1][j-1][k+2] + A[t%2][i-1][j][k] + A[t%2][i-1][j+1][k-2] + A[t%2][i-1][j+1][k+2] + A[t%2][i-1][j+2][k-1] + A[t%2][i-1][j+2][k+1] + A[t%2][i][j-1][k-1] + A[t%2][i][j-1][k+1] + A[t%2][i][j+1][k-1] + A[t%2][i][j+1][k+1] + A[t%2][i+1][j-2][k-1] + A[t%2][i+1][j-2][k+1] + A[t%2][i+1][j-1][k-2] + A[t%2][i+1][j-1][k+2] + A[t%2][i+1][j][k] + A[t%2][i+1][j+1][k-2] + A[t%2][i+1][j+1][k+2] + A[t%2][i+1][j+2][k-1] + A[t%2][i+1][j+2][k+1])
+            + c6 * (double)(A[t%2][i-2][j-1][k-1] + A[t%2][i-2][j-1][k+1] + A[t%2][i-2][j+1][k-1] + A[t%2][i-2][j+1][k+1]));
+  }
+}
+
+void oracle_3d125pt_q(long double *A1, const int *n, int timestep,
+    const long double *coef, long double divisor, long double eps)
+{
+  (void)eps; (void)divisor;
+  const long d0 = n[0] + 4, d1 = n[1] + 4, d2 = n[2] + 4;
+  long double (*A)[d0][d1][d2] = (long double (*)[d0][d1][d2])A1;
+  const long double c0 = coef ? (long double)coef[0] : (long double)0.75;
+  const long double c1 = coef ? (long double)coef[16] : (long double)0.76;
+  const long double c2 = coef ? (long double)coef[20] : (long double)1.132;
+  const long double c3 = coef ? (long double)coef[50] : (long double)0.217;
+  const long double c4 = coef ? (long double)coef[70] : (long double)2.13;
+  const long double c5 = coef ? (long double)coef[95] : (long double)0.331;
+  const long double c6 = coef ? (long double)coef[121] : (long double)0.332;
+  for (int t = 0; t < timestep; t++) {
+#pragma omp parallel for schedule(static)
+    for (long i = 2; i < d0 - 2; i++)
+      for (long j = 2; j < d1 - 2; j++)
+        for (long k = 2; k < d2 - 2; k++)
+          A[(t+1)%2][i][j][k] = (long double)(c0 * (long double)(A[t%2][i-2][j-2][k-2] + A[t%2][i-2][j-2][k+2] + A[t%2][i-2][j+2][k-2] + A[t%2][i-2][j+2][k+2] + A[t%2][i-1][j-1][k-1] + A[t%2][i-1][j-1][k+1] + A[t%2][i-1][j+1][k-1] + A[t%2][i-1][j+1][k+1] + A[t%2][i][j-1][k] + A[t%2][i][j][k-1] + A[t%2][i][j][k+1] + A[t%2][i][j+1][k] + A[t%2][i+1][j-1][k-1] + A[t%2][i+1][j-1][k+1] + A[t%2][i+1][j+1][k-1] + A[t%2][i+1][j+1][k+1])
+            + c1 * (long double)(A[t%2][i-2][j-2][k-2] + A[t%2][i-2][j-2][k+2] + A[t%2][i-2][j+2][k-2] + A[t%2][i-2][j+2][k+2])
+            + c2 * (long double)(A[t%2][i-2][j-2][k-1] + A[t%2][i-2][j-2][k+1] + A[t%2][i-2][j-1][k-2] + A[t%2][i-2][j-1][k+2] + A[t%2][i-2][j][k] + A[t%2][i-2][j+1][k-2] + A[t%2][i-2][j+1][k+2] + A[t%2][i-2][j+2][k-1] + A[t%2][i-2][j+2][k+1] + A[t%2][i-1][j-2][k-2] + A[t%2][i-1][j-2][k+2] + A[t%2][i-1][j+2][k-2] + A[t%2][i-1][j+2][k+2] + A[t%2][i][j-2][k] + A[t%2][i][j][k-2] + A[t%2][i][j][k+2] + A[t%2][i][j+2][k] + A[t%2][i+1][j-2][k-2] + A[t%2][i+1][j-2][k+2] + A[t%2][i+1][j+2][k-2] + A[t%2][i+1][j+2][k+2] + A[t%2][i-2][j-2][k-1] + A[t%2][i-2][j-2][k+1] + A[t%2][i-2][j-1][k-2] + A[t%2][i-2][j-1][k+2] + A[t%2][i-2][j][k] + A[t%2][i-2][j+1][k-2] + A[t%2][i-2][j+1][k+2] + A[t%2][i-2][j+2][k-1] + A[t%2][i-2][j+2][k+1])
+            + c3 * (long double)(A[t%2][i-2][j-2][k] + A[t%2][i-2][j][k-2] + A[t%2][i-2][j][k+2] + A[t%2][i-2][j+2][k] + A[t%2][i-1][j-1][k] + A[t%2][i-1][j][k-1] + A[t%2][i-1][j][k+1] + A[t%2][i-1][j+1][k] + A[t%2][i][j-2][k-2] + A[t%2][i][j-2][k+2] + A[t%2][i][j+2][k-2] + A[t%2][i][j+2][k+2] + A[t%2][i+1][j-1][k] + A[t%2][i+1][j][k-1] + A[t%2][i+1][j][k+1] + A[t%2][i+1][j+1][k] + A[t%2][i-2][j-2][k] + A[t%2][i-2][j][k-2] + A[t%2][i-2][j][k+2] + A[t%2][i-2][j+2][k])
+            + c4 * (long double)(A[t%2][i-2][j-1][k] + A[t%2][i-2][j][k-1] + A[t%2][i-2][j][k+1] + A[t%2][i-2][j+1][k] + A[t%2][i-1][j-2][k] + A[t%2][i-1][j][k-2] + A[t%2][i-1][j][k+2] + A[t%2][i-1][j+2][k] + A[t%2][i][j-2][k-1] + A[t%2][i][j-2][k+1] + A[t%2][i][j-1][k-2] + A[t%2][i][j-1][k+2] + A[t%2][i][j][k] + A[t%2][i][j+1][k-2] + A[t%2][i][j+1][k+2] + A[t%2][i][j+2][k-1] + A[t%2][i][j+2][k+1] + A[t%2][i+1][j-2][k] + A[t%2][i+1][j][k-2] + A[t%2][i+1][j][k+2] + A[t%2][i+1][j+2][k] + A[t%2][i-2][j-1][k] + A[t%2][i-2][j][k-1] + A[t%2][i-2][j][k+1] + A[t%2][i-2][j+1][k])
+            + c5 * (long double)(A[t%2][i-2][j-1][k-1] + A[t%2][i-2][j-1][k+1] + A[t%2][i-2][j+1][k-1] + A[t%2][i-2][j+1][k+1] + A[t%2][i-1][j-2][k-1] + A[t%2][i-1][j-2][k+1] + A[t%2][i-1][j-1][k-2] + A[t%2][i-1][j-1][k+2] + A[t%2][i-1][j][k] + A[t%2][i-1][j+1][k-2] + A[t%2][i-1][j+1][k+2] + A[t%2][i-1][j+2][k-1] + A[t%2][i-1][j+2][k+1] + A[t%2][i][j-1][k-1] + A[t%2][i][j-1][k+1] + A[t%2][i][j+1][k-1] + A[t%2][i][j+1][k+1] + A[t%2][i+1][j-2][k-1] + A[t%2][i+1][j-2][k+1] + A[t%2][i+1][j-1][k-2] + A[t%2][i+1][j-1][k+2] + A[t%2][i+1][j][k] + A[t%2][i+1][j+1][k-2] + A[t%2][i+1][j+1][k+2] + A[t%2][i+1][j+2][k-1] + A[t%2][i+1][j+2][k+1])
+            + c6 * (long double)(A[t%2][i-2][j-1][k-1] + A[t%2][i-2][j-1][k+1] + A[t%2][i-2][j+1][k-1] + A[t%2][i-2][j+1][k+1]));
+  }
+}
+
 typedef void (*oracle_fn_f)(float *, const int *, int, const float *, float, float);
 const oracle_fn_f oracle_table_f[] = {
   oracle_star2d1r_f,
@@ -5591,6 +5675,7 @@ const oracle_fn_f oracle_table_f[] = {
   oracle_box3d3r_f,
   oracle_box3d4r_f,
   oracle_j3d27pt_f,
+  oracle_3d125pt_f,
 };
 
 typedef void (*oracle_fn_d)(double *, const int *, int, const double *, double, double);
@@ -5616,6 +5701,7 @@ const oracle_fn_d oracle_table_d[] = {
   oracle_box3d3r_d,
   oracle_box3d4r_d,
   oracle_j3d27pt_d,
+  oracle_3d125pt_d,
 };
 
 typedef void (*oracle_fn_q)(long double *, const int *, int, const long double *, long double, long double);
@@ -5641,4 +5727,5 @@ const oracle_fn_q oracle_table_q[] = {
   oracle_box3d3r_q,
   oracle_box3d4r_q,
   oracle_j3d27pt_q,
+  oracle_3d125pt_q,
 };

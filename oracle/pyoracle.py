@@ -56,6 +56,8 @@ def reference_coefficients(name: str, dtype) -> np.ndarray:
     _, s = BY_NAME[name]
     if s["kind"] == "gradient":
         return np.array([np.float32(s["numerator"])], dtype=dtype)
+    if s.get("groups"):  # double literals (3d125pt)
+        return np.array([t["value"] for t in s["terms"]], dtype=dtype)
     return np.array([np.float32(t["value"]) for t in s["terms"]], dtype=dtype)
 
 
@@ -95,15 +97,20 @@ def run(name: str, A: np.ndarray, n, timestep: int, coef=None, divisor=None, eps
     if np.isscalar(n):
         n = [int(n)] * s["dim"]
     nn = (ctypes.c_int * 3)(*(list(n) + [0] * (3 - len(n))))
-    if coef is None:
+    coef_ptr = None
+    if coef is None and s.get("groups"):
+        coef_ptr = 0  # the grouped form's double literals, as the source writes them
+    elif coef is None:
         coef = reference_coefficients(name, A.dtype)
-    coef = np.ascontiguousarray(coef, dtype=A.dtype)
+    if coef_ptr is None:
+        coef = np.ascontiguousarray(coef, dtype=A.dtype)
+        coef_ptr = coef.ctypes.data
     if divisor is None:
         divisor = reference_divisor(name)
     if eps is None:
         eps = reference_eps(name)
     lib().oracle_run(sid, TCODE[A.dtype], A.ctypes.data, nn, int(timestep),
-                     coef.ctypes.data, float(divisor), float(eps))
+                     coef_ptr or None, float(divisor), float(eps))
     return A
 
 

@@ -40,14 +40,15 @@ def test_binding_covers_declarations():
 def test_catalogue_matches_table():
     L = capi.lib()
     table = json.loads((ROOT / "an5d-artifact_gb300" / "gbstencil" / "stencils.json").read_text())["stencils"]
-    assert L.gbs_num_stencils() == len(table) == 21
+    assert L.gbs_num_stencils() == len(table) == 22
     for i, s in enumerate(table):
         assert L.gbs_stencil_name(i).decode() == s["name"]
         assert L.gbs_stencil_id(s["name"].encode()) == i
         dim, rad, nt, fpp = (ctypes.c_int() for _ in range(4))
         capi.check(L.gbs_stencil_info(i, ctypes.byref(dim), ctypes.byref(rad), ctypes.byref(nt), ctypes.byref(fpp)))
         assert (dim.value, rad.value, fpp.value) == (s["dim"], s["rad"], s["fpp"])
-    assert L.gbs_stencil_id(b"3d125pt") == -1
+    assert L.gbs_stencil_id(b"3d125pt") == 21
+    assert L.gbs_stencil_id(b"3d999pt") == -1
 
 
 @pytest.mark.parametrize("name,dt,n", [("star2d1r", np.float32, 4096), ("star2d4r", np.float64, 77),

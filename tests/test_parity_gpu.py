@@ -23,9 +23,27 @@ NAMES_2D = [s["name"] for s in capi.TABLE if s["dim"] == 2]
 NAMES_3D = [s["name"] for s in capi.TABLE if s["dim"] == 3]
 
 
+def has_exact(name):
+    """3d125pt has no exact form in the engine (its float build sums groups
+    in float and combines them in double)."""
+    return capi.info(name).get("exact", True)
+
+
 def max_class(name, dt, mode):
-    """Largest fused degree the build instantiates (mirrors csrc/inst.cu)."""
+    """Largest fused degree the build instantiates (mirrors csrc/inst.cu);
+    0 when the mode is not built for the stencil."""
     s = capi.info(name)
+    if mode == "exact" and not has_exact(name):
+        return 0
+    if s.get("groups"):  # degrees limited by shared memory: ask the planner
+        import ctypes
+        top = 0
+        for bt in range(1, 9):
+            d, _ = capi.make_desc(name, dt, 64, 2 * bt, mode, bt=bt)
+            if capi.lib().gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) != capi.GBS_OK:
+                break
+            top = bt
+        return top
     if s["dim"] == 3:
         if s["rad"] >= 3:
             return 1
@@ -125,10 +143,20 @@ def test_parity_2d_random_coefficients(name):
 @pytest.mark.parametrize("case", GOLDEN,
                          ids=lambda c: f"{c['stencil']}-{c['dtype']}-{c['compsize']}-{c['timestep']}")
 def test_exact_mode_matches_artifact_golden(case):
-    """Bit-identical to the artifact's own CPU path (committed digests)."""
+    """Bit-identical to the artifact's own CPU path (committed digests). A
+    stencil without an exact form: FMA mode within tolerance of the oracle,
+    whose result carries the artifact's digest."""
     name, dt = case["stencil"], DT[case["dtype"]]
     n, T = case["compsize"], case["timestep"]
     A = po.init_grid(name, n, dt)
+    if not has_exact(name):
+        ref = A.copy()
+        po.run(name, ref, n, T)
+        assert hashlib.sha256(np.ascontiguousarray(ref[T % 2]).tobytes()).hexdigest() == case["sha256"]
+        d, _ = capi.make_desc(name, dt, n, T, fp_mode="fma")
+        capi.run_host(d, A)
+        assert po.normwise_error(A, ref, T) <= TOL[np.dtype(dt)]
+        return
     d, _ = capi.make_desc(name, dt, n, T, fp_mode="exact")
     capi.run_host(d, A)
     assert hashlib.sha256(np.ascontiguousarray(A[T % 2]).tobytes()).hexdigest() == case["sha256"]
@@ -144,6 +172,13 @@ CASES_3D = [  # (n, T, sl)
 @pytest.mark.parametrize("name", NAMES_3D)
 def test_parity_3d(name, dt, mode):
     mc = max_class(name, dt, mode)
+    if mc == 0:  # not built: refused, not computed
+        d, _ = capi.make_desc(name, dt, 11, 2, fp_mode=mode)
+        A = np.zeros(po.grid_shape(name, 11)[0], dt)
+        with pytest.raises(capi.GbsError) as e:
+            capi.run_host(d, A)
+        assert e.value.status == capi.GBS_ERR_UNSUPPORTED
+        return
     seed = 100
     for n, T, sl in CASES_3D:
         for bt in sorted({1, mc, 2 if mc >= 2 else 1}):
@@ -157,5 +192,6 @@ def test_parity_3d(name, dt, mode):
 def test_parity_3d_reference_init(name, dt):
     n, T = 40, 5
     A0 = po.init_grid(name, n, dt)
-    compare(name, A0, [n, n, n], T, dt, "exact", max_class(name, dt, "exact"))
+    if has_exact(name):
+        compare(name, A0, [n, n, n], T, dt, "exact", max_class(name, dt, "exact"))
     compare(name, A0, [n, n, n], T, dt, "fma", max_class(name, dt, "fma"))
