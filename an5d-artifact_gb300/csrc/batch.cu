@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -613,12 +614,24 @@ namespace gbs {
 namespace {
 // GBS_BATCH_STREAMS: each grid's own time loop (the engine's plain kernels at
 // the tuned degree) captured as a chain of kernel nodes; the chains are
-// spread over kStreams capture streams, heaviest first onto the least loaded
-// one, so independent grids run side by side. One graph launch.
-constexpr int kStreams = 16;
+// spread over kStreams capture streams (branches of the graph), heaviest
+// first onto the least loaded one, so independent grids run side by side.
+// Each grid's stream length is sized for its share of the GPU (one wave of
+// resident warps divided by the branches) instead of a whole wave, so that
+// a small grid's kernel leaves the SMs to the other branches. One graph
+// launch. GBS_BATCH_BRANCHES (environment, 1..64) overrides kStreams.
+constexpr int kStreams = 32;
+constexpr int kMaxStreams = 64;
+
+int branches() {
+  const char *e = std::getenv("GBS_BATCH_BRANCHES");
+  const int n = e ? std::atoi(e) : kStreams;
+  return n >= 1 && n <= kMaxStreams ? n : kStreams;
+}
 
 gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, gbs_batch **out) {
   if (!grids || ngrids <= 0) return fail(GBS_ERR_INVALID, "batch: no grids");
+  const int nbr = branches();
   std::vector<gbs_desc> ds(ngrids);
   std::vector<double> work(ngrids);
   long long cells = 0;
@@ -646,6 +659,15 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
     if (st != GBS_OK) return st;
     gbs_plan_info pi;
     if ((st = gbs_plan(&d, &pi)) != GBS_OK) return st;
+    // stream length for this grid's share of one wave
+    d.bt = pi.bt;
+    if (d.sl == 0) {
+      const Layout L = make_layout(&d);
+      const int fma = fp_mode == GBS_FP_FMA ? 1 : 0;
+      const long long share = std::max<long long>(1, resident_warps_2d(d.stencil, GBS_F32, fma, pi.bt) / nbr);
+      d.sl = geometry2d(L, pi.bt, 0, share).sl;
+      if ((st = gbs_plan(&d, &pi)) != GBS_OK) return st;
+    }
     launches += pi.launches;
     cells += (long long)bg.n[0] * bg.n[1] * bg.timestep;
     work[g] = (double)bg.n[0] * bg.n[1] * bg.timestep;
@@ -661,14 +683,14 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
   h->cells = cells;
   h->launches_plain = launches;
   h->mode = GBS_BATCH_STREAMS;
-  cudaStream_t cs = nullptr, side[kStreams] = {};
-  cudaEvent_t fork = nullptr, join[kStreams] = {};
+  cudaStream_t cs = nullptr, side[kMaxStreams] = {};
+  cudaEvent_t fork = nullptr, join[kMaxStreams] = {};
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-  for (int k = 0; k < kStreams && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking);
+  for (int k = 0; k < nbr && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
-  for (int k = 0; k < kStreams && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming);
+  for (int k = 0; k < nbr && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming);
   auto release = [&]() {
-    for (int k = 0; k < kStreams; ++k) {
+    for (int k = 0; k < kMaxStreams; ++k) {
       if (join[k]) cudaEventDestroy(join[k]);
       if (side[k]) cudaStreamDestroy(side[k]);
     }
@@ -684,16 +706,16 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaEventRecord(fork, cs);
-    for (int k = 0; k < kStreams; ++k) cudaStreamWaitEvent(side[k], fork, 0);
-    double load[kStreams] = {};
+    for (int k = 0; k < nbr; ++k) cudaStreamWaitEvent(side[k], fork, 0);
+    double load[kMaxStreams] = {};
     for (int g : order) {
-      const int k = (int)(std::min_element(load, load + kStreams) - load);
+      const int k = (int)(std::min_element(load, load + nbr) - load);
       load[k] += work[g];
       const Layout L = make_layout(&ds[g]);
       st = run_loop(&ds[g], L, grids[g].dev_A, side[k], err);
       if (st != GBS_OK) break;
     }
-    for (int k = 0; k < kStreams; ++k) {
+    for (int k = 0; k < nbr; ++k) {
       cudaEventRecord(join[k], side[k]);
       cudaStreamWaitEvent(cs, join[k], 0);
     }
