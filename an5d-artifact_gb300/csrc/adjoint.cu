@@ -223,6 +223,84 @@ __global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant
   }
 }
 
+// 2-D linear adjoint step, fused: lam_out(y) = sum_k c_k/d lam(y - o_k) on
+// the interior (lam is zero on the halo; lam_out's halo is never written),
+// hg(h) += the same sum at halo cells h, and with WANT_COEF the products
+// lam(y) u(y + o_k) / d summed per thread and reduced per CTA into
+// part[blockIdx.x][k]. One launch per step instead of the transposed engine
+// step, the halo kernel and the product kernel: 2-D grids are small enough
+// that the step is bound by kernel latency, not by traffic. Work units:
+// (row, 128-column segment), four columns per lane.
+template <class ST, typename T, bool WANT_COEF>
+__global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constant__ AdjGeom g, const T *lam,
+                                                            const T *u, T *lam_out, T *hg, double *part,
+                                                            const __grid_constant__ LinCoef<T, ST::kTerms> cf,
+                                                            T inv_div) {
+  constexpr int NT = ST::kTerms;
+  constexpr int NP = WANT_COEF ? NT : 1;
+  constexpr int SEG = 128;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int R = g.rad;
+  const long long nseg = (g.last + SEG - 1) / SEG;
+  const long long units = (long long)g.d0 * nseg;
+  const long long nwarps = ((long long)gridDim.x * kAdjThreads) >> 5;
+  T acc[NP];
+#pragma unroll
+  for (int t = 0; t < NP; ++t) acc[t] = T(0);
+  for (long long un = ((long long)blockIdx.x * kAdjThreads + threadIdx.x) >> 5; un < units; un += nwarps) {
+    const int i = (int)(un / nseg), seg = (int)(un - (long long)i * nseg);
+    const bool irow = i >= R && i < g.d0 - R;
+    const long long row = (long long)i * g.pitch + g.shift;
+#pragma unroll
+    for (int q = 0; q < SEG / 32; ++q) {
+      const int c = seg * SEG + q * 32 + lane;
+      if (c >= g.last) continue;
+      const bool in = irow && c >= R && c < g.last - R;
+      T s = T(0);
+      if (in) {
+        static_for<NT>([&](auto TI) {
+          constexpr int t = decltype(TI)::value;
+          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+          s = fma(cf.c[t], lam[row + c - (long long)di * g.pitch - dj], s);
+        });
+        lam_out[row + c] = s;
+        if constexpr (WANT_COEF) {
+          const T l = lam[row + c];
+          static_for<NT>([&](auto TI) {
+            constexpr int t = decltype(TI)::value;
+            constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+            acc[t] = fma(l, u[row + c + (long long)di * g.pitch + dj], acc[t]);
+          });
+        }
+      } else {
+        static_for<NT>([&](auto TI) {
+          constexpr int t = decltype(TI)::value;
+          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+          s = fma(cf.c[t], ldz(lam, g, i - di, 0, c - dj), s);
+        });
+        hg[row + c] += s;
+      }
+    }
+  }
+  if constexpr (WANT_COEF) {
+    __shared__ double red[kAdjThreads / 32][NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      T v = acc[t];
+#pragma unroll
+      for (int sh = 16; sh > 0; sh >>= 1) v += __shfl_down_sync(0xffffffffu, v, sh);
+      if (lane == 0) red[w][t] = (double)v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NT) {
+      double sum = 0.0;
+#pragma unroll
+      for (int ww = 0; ww < kAdjThreads / 32; ++ww) sum += red[ww][threadIdx.x];
+      part[(size_t)blockIdx.x * NT + threadIdx.x] += sum * (double)inv_div;
+    }
+  }
+}
+
 // gradient2d pre-pass: for interior x, q(x) = (eps + s(x))^{-1/2} and
 // sd(x) = sum_n d_n(x), d_n = u(x) - u(x + n), from u_t (s formed as the
 // forward step forms it)
@@ -450,6 +528,8 @@ bool transposed_coefficients(const gbs_stencil_def_t *s, const std::vector<doubl
 
 // kernels of one stencil and dtype
 struct AdjKernels {
+  cudaError_t (*fused2d)(const AdjGeom &, const void *, const void *, void *, void *, double *,
+                         const std::vector<double> &, double, bool, cudaStream_t);
   cudaError_t (*halo)(const AdjGeom &, const void *, void *, const std::vector<double> &, double, cudaStream_t);
   cudaError_t (*coef)(const AdjGeom &, const void *, const void *, double *, double, cudaStream_t);
   cudaError_t (*grad)(const AdjGeom &, const void *, void *, void *, const void *, void *, void *, double *, double,
@@ -473,6 +553,28 @@ cudaError_t run_halo(const AdjGeom &g, const void *lam, void *hg, const std::vec
     const double dv = ST::kHasDiv ? div : 1.0;
     for (int t = 0; t < ST::kTerms; ++t) cf.c[t] = (T)(coef[t] / dv);
     halo_kernel<ST, T><<<halo_grid(g), kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<T *>(hg), cf);
+    return cudaGetLastError();
+  }
+}
+
+template <class ST, typename T>
+cudaError_t run_fused2d(const AdjGeom &g, const void *lam, const void *u, void *lam_out, void *hg, double *part,
+                        const std::vector<double> &coef, double div, bool want_coef, cudaStream_t s) {
+  if constexpr (ST::kKind == KIND_GRADIENT || ST::kDim != 2 || ST::kTerms > kMaxCoefGrad) {
+    return cudaErrorInvalidValue;
+  } else {
+    LinCoef<T, ST::kTerms> cf;
+    const double dv = ST::kHasDiv ? div : 1.0;
+    for (int t = 0; t < ST::kTerms; ++t) cf.c[t] = (T)(coef[t] / dv);
+    const T inv = (T)(1.0 / dv);
+    if (want_coef)
+      adj2d_kernel<ST, T, true><<<kCoefBlocks, kAdjThreads, 0, s>>>(
+          g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
+          part, cf, inv);
+    else
+      adj2d_kernel<ST, T, false><<<kCoefBlocks, kAdjThreads, 0, s>>>(
+          g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
+          part, cf, inv);
     return cudaGetLastError();
   }
 }
@@ -510,12 +612,14 @@ AdjKernels adj_kernels(int sid, int dtype) {
   switch (sid) {
 #define GBS_ADJ(id, S)                                                                            \
   case id:                                                                                         \
-    return dtype == GBS_F64 ? AdjKernels{&run_halo<S, double>, &run_coef<S, double>, &run_grad<S, double>} \
-                            : AdjKernels{&run_halo<S, float>, &run_coef<S, float>, &run_grad<S, float>};
+    return dtype == GBS_F64                                                                       \
+               ? AdjKernels{&run_fused2d<S, double>, &run_halo<S, double>, &run_coef<S, double>,      \
+                            &run_grad<S, double>}                                                       \
+               : AdjKernels{&run_fused2d<S, float>, &run_halo<S, float>, &run_coef<S, float>, &run_grad<S, float>};
     GBS_FOR_EACH_STENCIL(GBS_ADJ)
 #undef GBS_ADJ
     default:
-      return AdjKernels{nullptr, nullptr, nullptr};
+      return AdjKernels{nullptr, nullptr, nullptr, nullptr};
   }
 }
 
@@ -623,6 +727,9 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
       CK(K.grad(g, u, ws + w.off_q, ws + w.off_sd, lam[cur], lam[cur ^ 1], hg, part, coef[0], eps,
                 dev_coef_grad != nullptr, s),
          "adjoint: gradient2d step");
+    } else if (g.dim == 2 && sd->nterms <= kMaxCoefGrad) {
+      CK(K.fused2d(g, lam[cur], u, lam[cur ^ 1], hg, part, coef, div, dev_coef_grad != nullptr, s),
+         "adjoint: fused 2-D step");
     } else {
       CK(K.halo(g, lam[cur], hg, coef, div, s), "adjoint: halo");
       if (dev_coef_grad) CK(K.coef(g, lam[cur], u, part, div, s), "adjoint: coefficients");
