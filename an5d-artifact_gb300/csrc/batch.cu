@@ -659,9 +659,11 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
     if (st != GBS_OK) return st;
     gbs_plan_info pi;
     if ((st = gbs_plan(&d, &pi)) != GBS_OK) return st;
-    // stream length for this grid's share of one wave
+    // stream length for this grid's share of one wave (GBS_BATCH_SHARE=0:
+    // the single-grid choice, one whole wave per kernel)
     d.bt = pi.bt;
-    if (d.sl == 0) {
+    const char *share_env = std::getenv("GBS_BATCH_SHARE");
+    if (d.sl == 0 && !(share_env && share_env[0] == '0')) {
       const Layout L = make_layout(&d);
       const int fma = fp_mode == GBS_FP_FMA ? 1 : 0;
       const long long share = std::max<long long>(1, resident_warps_2d(d.stencil, GBS_F32, fma, pi.bt) / nbr);
