@@ -232,13 +232,16 @@ __global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant
 // that the step is bound by kernel latency, not by traffic. Work units:
 // (row, 128-column segment), four columns per lane.
 template <class ST, typename T, bool WANT_COEF>
-__global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constant__ AdjGeom g, const T *lam,
-                                                            const T *u, T *lam_out, T *hg, double *part,
+__global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constant__ AdjGeom g,
+                                                            const T *__restrict__ lam, const T *__restrict__ u,
+                                                            T *__restrict__ lam_out, T *__restrict__ hg,
+                                                            double *__restrict__ part,
                                                             const __grid_constant__ LinCoef<T, ST::kTerms> cf,
                                                             T inv_div) {
   constexpr int NT = ST::kTerms;
   constexpr int NP = WANT_COEF ? NT : 1;
-  constexpr int SEG = 128;
+  constexpr int Q = 4;           // columns per lane per unit
+  constexpr int SEG = 32 * Q;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int R = g.rad;
   const long long nseg = (g.last + SEG - 1) / SEG;
@@ -251,19 +254,21 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
     const int i = (int)(un / nseg), seg = (int)(un - (long long)i * nseg);
     const bool irow = i >= R && i < g.d0 - R;
     const long long row = (long long)i * g.pitch + g.shift;
+    // every load of the unit first (Q independent columns in flight), then the stores
+    T s[Q];
+    bool in[Q], valid[Q];
 #pragma unroll
-    for (int q = 0; q < SEG / 32; ++q) {
+    for (int q = 0; q < Q; ++q) {
       const int c = seg * SEG + q * 32 + lane;
-      if (c >= g.last) continue;
-      const bool in = irow && c >= R && c < g.last - R;
-      T s = T(0);
-      if (in) {
+      valid[q] = c < g.last;
+      in[q] = valid[q] && irow && c >= R && c < g.last - R;
+      s[q] = T(0);
+      if (in[q]) {
         static_for<NT>([&](auto TI) {
           constexpr int t = decltype(TI)::value;
           constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-          s = fma(cf.c[t], lam[row + c - (long long)di * g.pitch - dj], s);
+          s[q] = fma(cf.c[t], lam[row + c - (long long)di * g.pitch - dj], s[q]);
         });
-        lam_out[row + c] = s;
         if constexpr (WANT_COEF) {
           const T l = lam[row + c];
           static_for<NT>([&](auto TI) {
@@ -272,14 +277,19 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
             acc[t] = fma(l, u[row + c + (long long)di * g.pitch + dj], acc[t]);
           });
         }
-      } else {
+      } else if (valid[q]) {
         static_for<NT>([&](auto TI) {
           constexpr int t = decltype(TI)::value;
           constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-          s = fma(cf.c[t], ldz(lam, g, i - di, 0, c - dj), s);
+          s[q] = fma(cf.c[t], ldz(lam, g, i - di, 0, c - dj), s[q]);
         });
-        hg[row + c] += s;
       }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const long long o = row + seg * SEG + q * 32 + lane;
+      if (in[q]) lam_out[o] = s[q];
+      else if (valid[q]) hg[o] += s[q];
     }
   }
   if constexpr (WANT_COEF) {

@@ -616,11 +616,10 @@ namespace {
 // the tuned degree) captured as a chain of kernel nodes; the chains are
 // spread over kStreams capture streams (branches of the graph), heaviest
 // first onto the least loaded one, so independent grids run side by side.
-// Each grid's stream length is sized for its share of the GPU (one wave of
-// resident warps divided by the branches) instead of a whole wave, so that
-// a small grid's kernel leaves the SMs to the other branches. One graph
-// launch. GBS_BATCH_BRANCHES (environment, 1..64) overrides kStreams.
-constexpr int kStreams = 32;
+// One graph launch. GBS_BATCH_BRANCHES (environment, 1..64) overrides
+// kStreams; GBS_BATCH_SHARE=1 sizes each grid's stream length for a
+// branch's share of the GPU instead of a whole wave.
+constexpr int kStreams = 16;
 constexpr int kMaxStreams = 64;
 
 int branches() {
@@ -659,11 +658,12 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
     if (st != GBS_OK) return st;
     gbs_plan_info pi;
     if ((st = gbs_plan(&d, &pi)) != GBS_OK) return st;
-    // stream length for this grid's share of one wave (GBS_BATCH_SHARE=0:
-    // the single-grid choice, one whole wave per kernel)
+    // GBS_BATCH_SHARE=1: stream length for this grid's share of one wave
+    // (default: the single-grid choice, one whole wave per kernel, which
+    // measured faster on GB300: 254 vs 220 GCells/s at 16 branches)
     d.bt = pi.bt;
     const char *share_env = std::getenv("GBS_BATCH_SHARE");
-    if (d.sl == 0 && !(share_env && share_env[0] == '0')) {
+    if (d.sl == 0 && share_env && share_env[0] == '1') {
       const Layout L = make_layout(&d);
       const int fma = fp_mode == GBS_FP_FMA ? 1 : 0;
       const long long share = std::max<long long>(1, resident_warps_2d(d.stencil, GBS_F32, fma, pi.bt) / nbr);

@@ -197,11 +197,10 @@ typedef struct gbs_batch_stats {
  *   every grid's items of that block; kernel boundaries order the blocks, so
  *   nothing waits on the device.
  * GBS_BATCH_STREAMS: each grid's own time loop (the single-grid kernels at
- *   the tuned degree, one kernel node per fused launch, stream length sized
- *   for the grid's share of the GPU) as a chain in the graph; the chains are
- *   spread over 32 branches (environment GBS_BATCH_BRANCHES, 1..64),
- *   heaviest grid first onto the least loaded branch, so independent grids
- *   run side by side. */
+ *   the tuned degree, one kernel node per fused launch) as a chain in the
+ *   graph; the chains are spread over 16 branches (environment
+ *   GBS_BATCH_BRANCHES, 1..64), heaviest grid first onto the least loaded
+ *   branch, so independent grids run side by side. */
 enum { GBS_BATCH_PERSISTENT = 0, GBS_BATCH_LAYERED = 1, GBS_BATCH_STREAMS = 2 };
 
 /* Plans the batch: work items, per-grid dependency counters and the CUDA
