@@ -108,50 +108,54 @@ __host__ __device__ inline HaloPlan halo_plan(const AdjGeom &g) {
   return h;
 }
 
-// hg(h) += sum_k c_k/d lam(h - o_k) for every halo cell h
-template <class ST, typename T>
-__global__ void __launch_bounds__(kAdjThreads) halo_kernel(const __grid_constant__ AdjGeom g, const T *lam, T *hg,
-                                                           const __grid_constant__ LinCoef<T, ST::kTerms> cf) {
-  const HaloPlan hp = halo_plan(g);
+// halo cell number tid of the enumeration above: (i, j, c); false past the end
+__device__ __forceinline__ bool halo_cell(const AdjGeom &g, const HaloPlan &hp, long long tid, int &i, int &j,
+                                          int &c) {
   const int R = g.rad;
-  const long long tid = (long long)blockIdx.x * kAdjThreads + threadIdx.x;
-  int i, j = 0, c;
+  j = 0;
   if (tid < hp.na) {
     const long long row = tid / (2 * R);
     const int e = (int)(tid - row * 2 * R);
     if (g.dim == 2) {
-      if (row >= g.d0 - 2 * R) return;
+      if (row >= g.d0 - 2 * R) return false;
       i = R + (int)row;
     } else {
       const int w1 = g.d1 - 2 * R;
-      if (row >= (long long)(g.d0 - 2 * R) * w1) return;
+      if (row >= (long long)(g.d0 - 2 * R) * w1) return false;
       i = R + (int)(row / w1);
       j = R + (int)(row - (long long)(i - R) * w1);
     }
     c = e < R ? e : g.last - 2 * R + e;
+    return true;
+  }
+  const long long b = tid - hp.na;
+  const long long wrow = (b >> 5) / hp.nseg;
+  const int seg = (int)((b >> 5) - wrow * hp.nseg);
+  if (wrow >= hp.rows_b) return false;
+  c = seg * 32 + (int)(b & 31);
+  if (c >= g.last) return false;
+  if (g.dim == 2) {
+    i = wrow < R ? (int)wrow : g.d0 - 2 * R + (int)wrow;
   } else {
-    const long long b = tid - hp.na;
-    const long long wrow = (b >> 5) / hp.nseg;
-    const int seg = (int)((b >> 5) - wrow * hp.nseg);
-    if (wrow >= hp.rows_b) return;
-    c = seg * 32 + (int)(b & 31);
-    if (c >= g.last) return;
-    if (g.dim == 2) {
-      i = wrow < R ? (int)wrow : g.d0 - 2 * R + (int)wrow;
+    const long long full = 2LL * R * g.d1;  // rows of the all-halo planes
+    if (wrow < full) {
+      const int p = (int)(wrow / g.d1);
+      i = p < R ? p : g.d0 - 2 * R + p;
+      j = (int)(wrow - (long long)p * g.d1);
     } else {
-      const long long full = 2LL * R * g.d1;  // rows of the all-halo planes
-      if (wrow < full) {
-        const int p = (int)(wrow / g.d1);
-        i = p < R ? p : g.d0 - 2 * R + p;
-        j = (int)(wrow - (long long)p * g.d1);
-      } else {
-        const long long q = wrow - full;
-        i = R + (int)(q / (2 * R));
-        const int jj = (int)(q - (long long)(i - R) * 2 * R);
-        j = jj < R ? jj : g.d1 - 2 * R + jj;
-      }
+      const long long q = wrow - full;
+      i = R + (int)(q / (2 * R));
+      const int jj = (int)(q - (long long)(i - R) * 2 * R);
+      j = jj < R ? jj : g.d1 - 2 * R + jj;
     }
   }
+  return true;
+}
+
+// hg(h) += sum_k c_k/d lam(h - o_k) at halo cell h
+template <class ST, typename T>
+__device__ __forceinline__ void halo_update(const AdjGeom &g, const T *lam, T *hg, const LinCoef<T, ST::kTerms> &cf,
+                                            int i, int j, int c) {
   T acc = T(0);
   static_for<ST::kTerms>([&](auto TI) {
     constexpr int t = decltype(TI)::value;
@@ -162,6 +166,16 @@ __global__ void __launch_bounds__(kAdjThreads) halo_kernel(const __grid_constant
   });
   const long long o = (ST::kDim == 2 ? (long long)i * g.pitch : ((long long)i * g.d1 + j) * g.pitch) + g.shift + c;
   hg[o] += acc;
+}
+
+// hg(h) += sum_k c_k/d lam(h - o_k) for every halo cell h
+template <class ST, typename T>
+__global__ void __launch_bounds__(kAdjThreads) halo_kernel(const __grid_constant__ AdjGeom g, const T *lam, T *hg,
+                                                           const __grid_constant__ LinCoef<T, ST::kTerms> cf) {
+  const HaloPlan hp = halo_plan(g);
+  int i, j, c;
+  if (halo_cell(g, hp, (long long)blockIdx.x * kAdjThreads + threadIdx.x, i, j, c))
+    halo_update<ST, T>(g, lam, hg, cf, i, j, c);
 }
 
 // part[blockIdx.x][k] += sum over interior x of lam(x) u(x + o_k) / d.
@@ -225,71 +239,92 @@ __global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant
 
 // 2-D linear adjoint step, fused: lam_out(y) = sum_k c_k/d lam(y - o_k) on
 // the interior (lam is zero on the halo; lam_out's halo is never written),
-// hg(h) += the same sum at halo cells h, and with WANT_COEF the products
-// lam(y) u(y + o_k) / d summed per thread and reduced per CTA into
-// part[blockIdx.x][k]. One launch per step instead of the transposed engine
+// with WANT_COEF the products lam(y) u(y + o_k) / d summed per thread and
+// reduced per CTA into part[blockIdx.x][k], and hg(h) += the transposed sum
+// at every halo cell h. One launch per step instead of the transposed engine
 // step, the halo kernel and the product kernel: 2-D grids are small enough
-// that the step is bound by kernel latency, not by traffic. Work units:
-// (row, 128-column segment), four columns per lane.
+// that a step is bound by kernel latency. The first `interior_blocks` CTAs
+// take (interior row, 32*V-column) units: each lane one aligned 16-byte
+// vector of V columns per row offset, the in-row neighbours from the
+// adjacent lanes (the warp's two edge lanes load theirs); the CTAs after
+// them take the halo cells (one thread each).
 template <class ST, typename T, bool WANT_COEF>
 __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constant__ AdjGeom g,
                                                             const T *__restrict__ lam, const T *__restrict__ u,
                                                             T *__restrict__ lam_out, T *__restrict__ hg,
                                                             double *__restrict__ part,
                                                             const __grid_constant__ LinCoef<T, ST::kTerms> cf,
-                                                            T inv_div) {
+                                                            T inv_div, int interior_blocks) {
   constexpr int NT = ST::kTerms;
   constexpr int NP = WANT_COEF ? NT : 1;
-  constexpr int Q = 4;           // columns per lane per unit
-  constexpr int SEG = 32 * Q;
+  constexpr int V = 16 / sizeof(T);
+  constexpr int R = ST::kRad;
+  constexpr int SEG = 32 * V;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int R = g.rad;
-  const long long nseg = (g.last + SEG - 1) / SEG;
-  const long long units = (long long)g.d0 * nseg;
-  const long long nwarps = ((long long)gridDim.x * kAdjThreads) >> 5;
+  if ((int)blockIdx.x >= interior_blocks) {
+    const HaloPlan hp = halo_plan(g);
+    int i, j, c;
+    if (halo_cell(g, hp, (long long)(blockIdx.x - interior_blocks) * kAdjThreads + threadIdx.x, i, j, c))
+      halo_update<ST, T>(g, lam, hg, cf, i, j, c);
+    return;
+  }
   T acc[NP];
 #pragma unroll
   for (int t = 0; t < NP; ++t) acc[t] = T(0);
-  for (long long un = ((long long)blockIdx.x * kAdjThreads + threadIdx.x) >> 5; un < units; un += nwarps) {
-    const int i = (int)(un / nseg), seg = (int)(un - (long long)i * nseg);
-    const bool irow = i >= R && i < g.d0 - R;
-    const long long row = (long long)i * g.pitch + g.shift;
-    // every load of the unit first (Q independent columns in flight), then the stores
-    T s[Q];
-    bool in[Q], valid[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int c = seg * SEG + q * 32 + lane;
-      valid[q] = c < g.last;
-      in[q] = valid[q] && irow && c >= R && c < g.last - R;
-      s[q] = T(0);
-      if (in[q]) {
-        static_for<NT>([&](auto TI) {
-          constexpr int t = decltype(TI)::value;
-          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-          s[q] = fma(cf.c[t], lam[row + c - (long long)di * g.pitch - dj], s[q]);
-        });
-        if constexpr (WANT_COEF) {
-          const T l = lam[row + c];
-          static_for<NT>([&](auto TI) {
-            constexpr int t = decltype(TI)::value;
-            constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-            acc[t] = fma(l, u[row + c + (long long)di * g.pitch + dj], acc[t]);
-          });
-        }
-      } else if (valid[q]) {
-        static_for<NT>([&](auto TI) {
-          constexpr int t = decltype(TI)::value;
-          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-          s[q] = fma(cf.c[t], ldz(lam, g, i - di, 0, c - dj), s[q]);
-        });
+  const int width = g.last - 2 * R;
+  const int nseg = (width + SEG - 1) / SEG;
+  const long long units = (long long)(g.d0 - 2 * R) * nseg;
+  const long long nwarps = (long long)interior_blocks * (kAdjThreads / 32);
+  for (long long un = (long long)blockIdx.x * (kAdjThreads / 32) + w; un < units; un += nwarps) {
+    const int ii = (int)(un / nseg), seg = (int)(un - (long long)ii * nseg);
+    const int i = R + ii;
+    const int c0 = R + seg * SEG + lane * V;        // the lane's first column; 16-byte aligned
+    const int nvalid = min(V, g.last - R - c0);     // columns of the group inside the interior
+    const long long base = (long long)i * g.pitch + g.shift + c0;
+    // element x (relative to c0, x in [-R, V+R)) of row offset dr of plane p
+    auto elem = [&](const T *p, auto DR, auto X) -> T {
+      constexpr int dr = decltype(DR)::value, x = decltype(X)::value;
+      const T *rp = p + base + (long long)dr * g.pitch;
+      T vec[V];
+      ld_vec<T, V>(vec, rp);
+      T v = row_elem<V, x>(vec);
+      if constexpr (x < 0) {
+        if (lane == 0) v = rp[x];
+      } else if constexpr (x >= V) {
+        if (lane == 31) v = rp[x];
       }
-    }
+      return v;
+    };
+    T sv[V];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const long long o = row + seg * SEG + q * 32 + lane;
-      if (in[q]) lam_out[o] = s[q];
-      else if (valid[q]) hg[o] += s[q];
+    for (int e = 0; e < V; ++e) sv[e] = T(0);
+    static_for<NT>([&](auto TI) {
+      constexpr int t = decltype(TI)::value;
+      constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+      static_for<V>([&](auto EI) {
+        constexpr int e = decltype(EI)::value;
+        sv[e] = fma(cf.c[t], elem(lam, IC<-di>(), IC<e - dj>()), sv[e]);
+      });
+    });
+    if constexpr (WANT_COEF) {
+      T lv[V];
+      ld_vec<T, V>(lv, lam + base);
+      static_for<NT>([&](auto TI) {
+        constexpr int t = decltype(TI)::value;
+        constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+        static_for<V>([&](auto EI) {
+          constexpr int e = decltype(EI)::value;
+          const T uv = elem(u, IC<di>(), IC<e + dj>());
+          if (e < nvalid) acc[t] = fma(lv[e], uv, acc[t]);
+        });
+      });
+    }
+    if (nvalid == V) {
+      st_vec<T, V>(lam_out + base, sv);
+    } else {
+#pragma unroll
+      for (int e = 0; e < V; ++e)
+        if (e < nvalid) lam_out[base + e] = sv[e];
     }
   }
   if constexpr (WANT_COEF) {
@@ -577,14 +612,17 @@ cudaError_t run_fused2d(const AdjGeom &g, const void *lam, const void *u, void *
     const double dv = ST::kHasDiv ? div : 1.0;
     for (int t = 0; t < ST::kTerms; ++t) cf.c[t] = (T)(coef[t] / dv);
     const T inv = (T)(1.0 / dv);
+    const HaloPlan hp = halo_plan(g);
+    const long long halo_threads = hp.na + hp.rows_b * hp.nseg * 32;
+    const unsigned grid = (unsigned)(kCoefBlocks + (halo_threads + kAdjThreads - 1) / kAdjThreads);
     if (want_coef)
-      adj2d_kernel<ST, T, true><<<kCoefBlocks, kAdjThreads, 0, s>>>(
+      adj2d_kernel<ST, T, true><<<grid, kAdjThreads, 0, s>>>(
           g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
-          part, cf, inv);
+          part, cf, inv, kCoefBlocks);
     else
-      adj2d_kernel<ST, T, false><<<kCoefBlocks, kAdjThreads, 0, s>>>(
+      adj2d_kernel<ST, T, false><<<grid, kAdjThreads, 0, s>>>(
           g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
-          part, cf, inv);
+          part, cf, inv, kCoefBlocks);
     return cudaGetLastError();
   }
 }
