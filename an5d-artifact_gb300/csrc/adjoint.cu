@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant
 // that a step is bound by kernel latency. The first `interior_blocks` CTAs
 // take (interior row, 32*V-column) units: each lane one aligned 16-byte
 // vector of V columns per row offset, the in-row neighbours from the
-// adjacent lanes (the warp's two edge lanes load theirs); the CTAs after
+// lanes up to R/V away (the warp's edge lanes load theirs); the CTAs after
 // them take the halo cells (one thread each).
 template <class ST, typename T, bool WANT_COEF>
 __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constant__ AdjGeom g,
@@ -288,10 +288,13 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
       T vec[V];
       ld_vec<T, V>(vec, rp);
       T v = row_elem<V, x>(vec);
+      // lanes whose neighbour lane (dl lanes away) is outside the warp load it
       if constexpr (x < 0) {
-        if (lane == 0) v = rp[x];
+        constexpr int dl = (-x + V - 1) / V;
+        if (lane < dl) v = rp[x];
       } else if constexpr (x >= V) {
-        if (lane == 31) v = rp[x];
+        constexpr int dl = x / V;
+        if (lane >= 32 - dl) v = rp[x];
       }
       return v;
     };
