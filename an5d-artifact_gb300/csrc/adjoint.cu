@@ -281,20 +281,24 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
     const int c0 = R + seg * SEG + lane * V;        // the lane's first column; 16-byte aligned
     const int nvalid = min(V, g.last - R - c0);     // columns of the group inside the interior
     const long long base = (long long)i * g.pitch + g.shift + c0;
-    // element x (relative to c0, x in [-R, V+R)) of row offset dr of plane p
-    auto elem = [&](const T *p, auto DR, auto X) -> T {
-      constexpr int dr = decltype(DR)::value, x = decltype(X)::value;
-      const T *rp = p + base + (long long)dr * g.pitch;
-      T vec[V];
-      ld_vec<T, V>(vec, rp);
-      T v = row_elem<V, x>(vec);
-      // lanes whose neighbour lane (dl lanes away) is outside the warp load it
+    // the 2R+1 row vectors of the unit, each loaded once
+    T lrow[2 * R + 1][V];
+    static_for<2 * R + 1>([&](auto DI) {
+      constexpr int d = decltype(DI)::value - R;
+      ld_vec<T, V>(lrow[d + R], lam + base + (long long)d * g.pitch);
+    });
+    // element x (relative to c0, x in [-R, V+R)) of row offset d: from the
+    // lane's own vector or a lane up to R/V away; lanes whose source lane is
+    // outside the warp load it
+    auto elem = [&](const T *p, const T (&rows)[2 * R + 1][V], auto D, auto X) -> T {
+      constexpr int d = decltype(D)::value, x = decltype(X)::value;
+      T v = row_elem<V, x>(rows[d + R]);
       if constexpr (x < 0) {
         constexpr int dl = (-x + V - 1) / V;
-        if (lane < dl) v = rp[x];
+        if (lane < dl) v = p[base + (long long)d * g.pitch + x];
       } else if constexpr (x >= V) {
         constexpr int dl = x / V;
-        if (lane >= 32 - dl) v = rp[x];
+        if (lane >= 32 - dl) v = p[base + (long long)d * g.pitch + x];
       }
       return v;
     };
@@ -306,19 +310,22 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
       constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
       static_for<V>([&](auto EI) {
         constexpr int e = decltype(EI)::value;
-        sv[e] = fma(cf.c[t], elem(lam, IC<-di>(), IC<e - dj>()), sv[e]);
+        sv[e] = fma(cf.c[t], elem(lam, lrow, IC<-di>(), IC<e - dj>()), sv[e]);
       });
     });
     if constexpr (WANT_COEF) {
-      T lv[V];
-      ld_vec<T, V>(lv, lam + base);
+      T urow[2 * R + 1][V];
+      static_for<2 * R + 1>([&](auto DI) {
+        constexpr int d = decltype(DI)::value - R;
+        ld_vec<T, V>(urow[d + R], u + base + (long long)d * g.pitch);
+      });
       static_for<NT>([&](auto TI) {
         constexpr int t = decltype(TI)::value;
         constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
         static_for<V>([&](auto EI) {
           constexpr int e = decltype(EI)::value;
-          const T uv = elem(u, IC<di>(), IC<e + dj>());
-          if (e < nvalid) acc[t] = fma(lv[e], uv, acc[t]);
+          const T uv = elem(u, urow, IC<di>(), IC<e + dj>());
+          if (e < nvalid) acc[t] = fma(lrow[R][e], uv, acc[t]);
         });
       });
     }
