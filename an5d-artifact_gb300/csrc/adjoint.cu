@@ -237,6 +237,24 @@ __global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant
   }
 }
 
+// Element x (relative to the lane's first column, x in [-R, V+R)) of row
+// offset D of a plane whose 2R+1 row vectors the lane holds: from its own
+// vector or from a lane up to R/V away; lanes whose source lane lies outside
+// the warp load the element.
+template <int V, int R, int D, int X, typename T>
+__device__ __forceinline__ T row_value(const T *p, const T (&rows)[2 * R + 1][V], long long base, long long pitch,
+                                       int lane) {
+  T v = row_elem<V, X>(rows[D + R]);
+  if constexpr (X < 0) {
+    constexpr int dl = (-X + V - 1) / V;
+    if (lane < dl) v = p[base + (long long)D * pitch + X];
+  } else if constexpr (X >= V) {
+    constexpr int dl = X / V;
+    if (lane >= 32 - dl) v = p[base + (long long)D * pitch + X];
+  }
+  return v;
+}
+
 // 2-D linear adjoint step, fused: lam_out(y) = sum_k c_k/d lam(y - o_k) on
 // the interior (lam is zero on the halo; lam_out's halo is never written),
 // with WANT_COEF the products lam(y) u(y + o_k) / d summed per thread and
@@ -287,21 +305,6 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
       constexpr int d = decltype(DI)::value - R;
       ld_vec<T, V>(lrow[d + R], lam + base + (long long)d * g.pitch);
     });
-    // element x (relative to c0, x in [-R, V+R)) of row offset d: from the
-    // lane's own vector or a lane up to R/V away; lanes whose source lane is
-    // outside the warp load it
-    auto elem = [&](const T *p, const T (&rows)[2 * R + 1][V], auto D, auto X) -> T {
-      constexpr int d = decltype(D)::value, x = decltype(X)::value;
-      T v = row_elem<V, x>(rows[d + R]);
-      if constexpr (x < 0) {
-        constexpr int dl = (-x + V - 1) / V;
-        if (lane < dl) v = p[base + (long long)d * g.pitch + x];
-      } else if constexpr (x >= V) {
-        constexpr int dl = x / V;
-        if (lane >= 32 - dl) v = p[base + (long long)d * g.pitch + x];
-      }
-      return v;
-    };
     T sv[V];
 #pragma unroll
     for (int e = 0; e < V; ++e) sv[e] = T(0);
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
       constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
       static_for<V>([&](auto EI) {
         constexpr int e = decltype(EI)::value;
-        sv[e] = fma(cf.c[t], elem(lam, lrow, IC<-di>(), IC<e - dj>()), sv[e]);
+        sv[e] = fma(cf.c[t], row_value<V, R, -di, e - dj>(lam, lrow, base, g.pitch, lane), sv[e]);
       });
     });
     if constexpr (WANT_COEF) {
@@ -324,7 +327,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
         constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
         static_for<V>([&](auto EI) {
           constexpr int e = decltype(EI)::value;
-          const T uv = elem(u, urow, IC<di>(), IC<e + dj>());
+          const T uv = row_value<V, R, di, e + dj>(u, urow, base, g.pitch, lane);
           if (e < nvalid) acc[t] = fma(lrow[R][e], uv, acc[t]);
         });
       });
