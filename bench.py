@@ -516,7 +516,13 @@ def run_adjoint(args, rank, world):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     cases, tot_cells, tot_bwd, tot_e2e, h2d, d2h, launches = [], 0, 0.0, 0.0, 0, 0, 0
     gen = torch.Generator(device=dev)
-    for ci, (name, dt, n, T, C, loss, want_coef) in enumerate(ADJOINT_CASES):
+    todo = list(ADJOINT_CASES)
+    if args.only:  # e.g. j2d5pt:float32 (small profiling cases)
+        keep = {tuple(x.split(":")) for x in args.only.split(",")}
+        todo = [c for c in todo if (c[0], np.dtype(c[1]).name) in keep][:1]
+    if args.T:
+        todo = [(a, b, c, args.T, min(e, args.T), f, g) for a, b, c, d, e, f, g in todo]
+    for ci, (name, dt, n, T, C, loss, want_coef) in enumerate(todo):
         tdt = torch.float32 if dt == np.float32 else torch.float64
         s = capi.info(name)
         shape = [x + 2 * s["rad"] for x in n]
@@ -567,19 +573,20 @@ def run_adjoint(args, rank, world):
                 bwd.append(e0.elapsed_time(e1))
                 ck.append(ck_ms)
         capi.sync(stream.cuda_stream)
-        # end to end: host u_0 in, forward with checkpoints, backward, host gradient out
-        hu0 = u0.cpu().pin_memory()
-        hgrad = torch.empty_like(hu0).pin_memory()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        du0 = hu0.to(dev, non_blocking=True)
-        run = Checkpointed(name, du0, T, C)
-        gu, gc = run.backward(lam_of(run.u_T), want_coef=want_coef)
-        hgrad.copy_(gu, non_blocking=True)
-        torch.cuda.synchronize()
-        tot_e2e += (time.perf_counter() - t0) * 1e3
-        h2d += hu0.numel() * hu0.element_size()
-        d2h += hgrad.numel() * hgrad.element_size()
+        if not args.no_e2e:
+            # end to end: host u_0 in, forward with checkpoints, backward, host gradient out
+            hu0 = u0.cpu().pin_memory()
+            hgrad = torch.empty_like(hu0).pin_memory()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            du0 = hu0.to(dev, non_blocking=True)
+            run = Checkpointed(name, du0, T, C)
+            gu, gc = run.backward(lam_of(run.u_T), want_coef=want_coef)
+            hgrad.copy_(gu, non_blocking=True)
+            torch.cuda.synchronize()
+            tot_e2e += (time.perf_counter() - t0) * 1e3
+            h2d += hu0.numel() * hu0.element_size()
+            d2h += hgrad.numel() * hgrad.element_size()
         del run
         torch.cuda.empty_cache()
         f_ms, b_ms, c_ms = statistics.median(fwd), statistics.median(bwd), statistics.median(ck)
@@ -612,8 +619,9 @@ def run_adjoint(args, rank, world):
                                                      f"T={c['T']} C={c['checkpoint_every']}" for c in cases],
                    "l2": "flushed between timed runs (512 MB write)", "parallelism": "replicas" if world > 1 else "single GPU"},
         "adjoint": cases,
-        "e2e": {"value": round(tot_cells / (tot_e2e * 1e-3) / 1e9, 3), "unit": "GCells/s (forward+backward, host buffers)",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": None if args.no_e2e else {
+            "value": round(tot_cells / (tot_e2e * 1e-3) / 1e9, 3), "unit": "GCells/s (forward+backward, host buffers)",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": None,
                      "kernel": f"backward of {dom['stencil']} {dom['dtype']} {'x'.join(map(str, dom['n']))}",
