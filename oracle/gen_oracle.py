@@ -1,6 +1,6 @@
 """Generate ``oracle_stencils.c``, the CPU oracle, from the stencil tap table.
 
-TEST INFRASTRUCTURE ONLY. The oracle is the checker for the CUDA engine: only
+TEST INFRASTRUCTURE ONLY. The oracle is the reference the CUDA engine is tested against: only
 ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
 use it. No product code path calls it.
 

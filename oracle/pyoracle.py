@@ -2,7 +2,7 @@
 CPU path built under ``_ref/``.
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and ``bench.py``'s CPU-baseline leg, as the checker. The engine never calls
+and ``bench.py``'s CPU-baseline leg, as the oracle. The engine never calls
 it.
 """
 from __future__ import annotations
