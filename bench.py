@@ -590,7 +590,16 @@ def run_adjoint(args, rank, world):
         del run
         torch.cuda.empty_cache()
         f_ms, b_ms, c_ms = statistics.median(fwd), statistics.median(bwd), statistics.median(ck)
-        per_step = 2 if s["kind"] != "gradient" and not want_coef else (4 if want_coef else 3)
+        # kernel launches per backward step: gradient2d recompute + pre-pass +
+        # gather; 2-D linear (<= 32 terms) the fused step (+ recompute for
+        # coefficients); 3-D linear halo + transposed step (+ recompute and
+        # product kernel for coefficients)
+        if s["kind"] == "gradient":
+            per_step = 3
+        elif s["dim"] == 2 and s["nterms"] <= 32:
+            per_step = 2 if want_coef else 1
+        else:
+            per_step = 4 if want_coef else 2
         launches += (T * per_step + plain.launches) * args.steps
         tot_cells += cells
         tot_bwd += b_ms
