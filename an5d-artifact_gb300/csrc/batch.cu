@@ -662,16 +662,6 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
     // (default: the single-grid choice, one whole wave per kernel, which
     // measured faster on GB300: 254 vs 220 GCells/s at 16 branches)
     d.bt = pi.bt;
-    // grids below GBS_BATCH_SMALL_CELLS interior cells take the largest
-    // fused degree built: their launches are latency-bound, so fewer, deeper
-    // launches finish sooner when other branches fill the GPU
-    if (const char *sc = std::getenv("GBS_BATCH_SMALL_CELLS")) {
-      const long long thr = std::atoll(sc);
-      if ((long long)bg.n[0] * bg.n[1] < thr) {
-        d.bt = max_bt(d.stencil, GBS_F32, fp_mode == GBS_FP_FMA ? 1 : 0);
-        if ((st = gbs_plan(&d, &pi)) != GBS_OK) return st;
-      }
-    }
     const char *share_env = std::getenv("GBS_BATCH_SHARE");
     if (d.sl == 0 && share_env && share_env[0] == '1') {
       const Layout L = make_layout(&d);
