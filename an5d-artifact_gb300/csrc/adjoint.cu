@@ -594,6 +594,21 @@ struct AdjKernels {
                       double, bool, cudaStream_t);
 };
 
+// CTAs of a grid-stride kernel: one wave of resident CTAs (at most
+// kCoefBlocks, the rows of the partial-sum table), so that no partial second
+// wave repeats the per-CTA latency
+template <class K>
+int one_wave(K kernel) {
+  int nb = 0, dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kAdjThreads, 0) != cudaSuccess || nb <= 0) {
+    (void)cudaGetLastError();
+    return kCoefBlocks;
+  }
+  return std::max(1, std::min(kCoefBlocks, nb * sms));
+}
+
 // one thread per halo cell of the interior rows, one warp per segment of an all-halo row
 unsigned halo_grid(const AdjGeom &g) {
   const HaloPlan h = halo_plan(g);
@@ -627,15 +642,17 @@ cudaError_t run_fused2d(const AdjGeom &g, const void *lam, const void *u, void *
     const T inv = (T)(1.0 / dv);
     const HaloPlan hp = halo_plan(g);
     const long long halo_threads = hp.na + hp.rows_b * hp.nseg * 32;
-    const unsigned grid = (unsigned)(kCoefBlocks + (halo_threads + kAdjThreads - 1) / kAdjThreads);
+    const unsigned halo_blocks = (unsigned)((halo_threads + kAdjThreads - 1) / kAdjThreads);
+    static const int wave_c = one_wave(adj2d_kernel<ST, T, true>);
+    static const int wave_n = one_wave(adj2d_kernel<ST, T, false>);
     if (want_coef)
-      adj2d_kernel<ST, T, true><<<grid, kAdjThreads, 0, s>>>(
+      adj2d_kernel<ST, T, true><<<wave_c + halo_blocks, kAdjThreads, 0, s>>>(
           g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
-          part, cf, inv, kCoefBlocks);
+          part, cf, inv, wave_c);
     else
-      adj2d_kernel<ST, T, false><<<grid, kAdjThreads, 0, s>>>(
+      adj2d_kernel<ST, T, false><<<wave_n + halo_blocks, kAdjThreads, 0, s>>>(
           g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
-          part, cf, inv, kCoefBlocks);
+          part, cf, inv, wave_n);
     return cudaGetLastError();
   }
 }
@@ -646,8 +663,9 @@ cudaError_t run_coef(const AdjGeom &g, const void *lam, const void *u, double *p
     return cudaErrorInvalidValue;
   } else {
     const double dv = ST::kHasDiv ? div : 1.0;
-    coef_kernel<ST, T><<<kCoefBlocks, kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<const T *>(u),
-                                                           part, (T)(1.0 / dv));
+    static const int wave = one_wave(coef_kernel<ST, T>);
+    coef_kernel<ST, T><<<wave, kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<const T *>(u), part,
+                                                    (T)(1.0 / dv));
     return cudaGetLastError();
   }
 }
