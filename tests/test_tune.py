@@ -97,3 +97,17 @@ def test_tune_times_candidates(fresh_table, name, dtype, n):
     torch.cuda.synchronize()
     capi.sync(0)
     assert torch.equal(a.plane(0), b.plane(0))
+
+
+def test_model_prefers_fusion_when_memory_bound():
+    """The model's memory term shrinks with bt; its time per step is positive
+    and finite for every degree the planner accepts (host arithmetic; without
+    a GPU the peak rates fall back to fixed GB300 figures)."""
+    times = []
+    for bt in (1, 2, 4):
+        d, _ = capi.make_desc("star2d1r", np.float32, 4096, 8 * bt, "fma", bt=bt)
+        ms = ctypes.c_double(0.0)
+        assert capi.lib().gbs_tune_model(ctypes.byref(d), ctypes.byref(ms)) == capi.GBS_OK
+        assert 0 < ms.value < 1e3
+        times.append(ms.value)
+    assert times[0] > times[1] > times[2]
