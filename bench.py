@@ -1,7 +1,7 @@
 """Benchmark of the stencil time loop on GB300 (one JSON line on stdout).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload suite3d|star2d1r] [--fp-mode fma|exact]
+                    [--workload suite3d|star2d1r|batched|adjoint] [--fp-mode fma|exact]
 
 A step is one full time loop (T timesteps) over each grid of the workload:
 
@@ -11,8 +11,14 @@ A step is one full time loop (T timesteps) over each grid of the workload:
 * batched: 512 independent fp32 2-D grids, sides log-uniform in [128, 4096]
   per axis, stencil uniform over star2d1r-4r, box2d1r-4r, j2d5pt, j2d9pt,
   T uniform in [16, 512], normalised random coefficients per grid, all
-  advanced by ONE persistent CUDA-graph launch; the line also reports the
-  same work done by per-grid plain launches, one grid after another.
+  advanced by ONE CUDA-graph launch (--batch-mode: streams, the default,
+  persistent or layered); the line also reports the same work done by
+  per-grid plain launches, one grid after another.
+* adjoint: the gradient of the time loop (gbs_adjoint_forward/backward):
+  j2d5pt f32 2048^2 T=1024 (checkpoints every 32, gradients of u_0 and the
+  coefficients), gradient2d f64 4096^2 T=512, j3d27pt f32 384^3 T=256 and
+  eight j3d27pt grids of 192^3..384^3 (gradients of u_0); the line reports
+  each backward against the plain forward loop.
 
 Inputs are synthetic: every cell (halo included) i.i.d. U[0,1) from a fixed
 seed, coefficients U[0,1) normalised to sum 1. ``value`` is GCells/s
@@ -654,7 +660,7 @@ def main():
     ap.add_argument("--T", type=int, default=0, help="timestep override")
     ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
-    ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "layered", "streams"],
+    ap.add_argument("--batch-mode", default="streams", choices=["persistent", "layered", "streams"],
                     help="batched workload: scheduling of the work items")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
