@@ -25,15 +25,17 @@ import re
 import sys
 from pathlib import Path
 
+TABLE = Path(__file__).resolve().parent.parent / "gbstencil" / "stencils.json"
+
 CALL = """  if (scop) {
-    /* GB300 engine (libgbstencil): the same time loop, exact arithmetic */
+    /* GB300 engine (libgbstencil): the same time loop, %(what)s */
     gbs_desc gd = {0};
     double gbs_ms = 0.0;
     gd.stencil = gbs_stencil_id("%(name)s");
     gd.dtype = sizeof(SB_TYPE) == sizeof(double) ? GBS_F64 : GBS_F32;
     for (int a = 0; a < BENCH_DIM; a++) gd.n[a] = compsize;
     gd.timestep = timestep;
-    gd.fp_mode = GBS_FP_EXACT;
+    gd.fp_mode = %(mode)s;
     if (gbs_run(&gd, A1, &gbs_ms) != GBS_OK) {
       fprintf(stderr, "gbstencil: %%s\\n", gbs_last_error());
       exit(EXIT_FAILURE);
@@ -49,7 +51,16 @@ def shim(name: str, src: str) -> str:
     m = re.search(r"^  if \(scop\) \{\n#pragma scop\n.*?^#pragma endscop\n  \}\n", src, re.S | re.M)
     if not m:
         raise ValueError(f"{name}: no scop branch of the expected shape")
-    out = src[:m.start()] + CALL % {"name": name} + src[m.end():]
+    # stencils without an exact form in the engine (3d125pt) run in FMA mode,
+    # which agrees with the CPU branch within the documented tolerance
+    import json
+    exact = True
+    if TABLE.exists():
+        recs = {r["name"]: r for r in json.loads(TABLE.read_text())["stencils"]}
+        exact = recs.get(name, {}).get("exact", True)
+    fill = {"name": name, "mode": "GBS_FP_EXACT" if exact else "GBS_FP_FMA",
+            "what": "exact arithmetic" if exact else "FMA mode (no exact form)"}
+    out = src[:m.start()] + CALL % fill + src[m.end():]
     inc = '#include "common.h"\n'
     if inc not in out:
         raise ValueError(f"{name}: no common.h include")

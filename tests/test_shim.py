@@ -30,13 +30,16 @@ def test_shim_rewrites_only_the_scop_branch():
     out = m.shim("star2d1r", src)
     assert '#include "gbstencil.h"' in out and "gbs_run(&gd, A1, &gbs_ms)" in out
     assert "#pragma scop" not in out and "cpu();" in out and 'gbs_stencil_id("star2d1r")' in out
+    assert "GBS_FP_EXACT" in out
+    assert "GBS_FP_FMA" in m.shim("3d125pt", src.replace("star2d1r", "3d125pt"))
     with pytest.raises(ValueError):
         m.shim("x", "int main(void) { return 0; }\n")
 
 
 @pytest.mark.skipif(not (ARTIFACT / "common.h").exists() or not shutil.which("gcc"),
                     reason="needs the artifact's sources and gcc")
-@pytest.mark.parametrize("name,prec", [("star2d1r", "float"), ("j3d27pt", "double"), ("gradient2d", "float")])
+@pytest.mark.parametrize("name,prec", [("star2d1r", "float"), ("j3d27pt", "double"), ("gradient2d", "float"),
+                                       ("3d125pt", "float")])
 def test_shim_compiles_and_links(tmp_path, name, prec):
     m = _gen()
     m.main([str(ARTIFACT), str(tmp_path), name])
