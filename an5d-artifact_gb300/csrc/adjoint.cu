@@ -529,7 +529,7 @@ Workspace workspace_of(const gbs_desc *d, const Layout &L, int C) {
   w.nt = grad ? 1 : std::min(s->nterms, kMaxCoefGrad);
   w.off_cp = 0;
   w.off_stash = w.off_cp + (size_t)w.ncp * w.plane_bytes;
-  w.off_lam = w.off_stash + (size_t)C * w.plane_bytes;
+  w.off_lam = w.off_stash + 2 * (size_t)C * w.plane_bytes;  // two stash buffers
   w.off_hg = w.off_lam + 2 * w.plane_bytes;
   w.off_q = w.off_hg + w.plane_bytes;
   w.off_sd = w.off_q + (grad ? w.plane_bytes : 0);
@@ -824,27 +824,73 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
     for (int t = d->timestep - 1; t >= 0; --t)
       if ((st = step(nullptr)) != GBS_OK) return st;
   } else {
-    // the halo of every stash slot: the fixed boundary (never rewritten)
-    for (int k = 0; k < w.C; ++k)
+    // Two stash buffers: while the adjoint steps of chunk j run on `s`, a
+    // second stream recomputes the states of chunk j-1 into the other
+    // buffer. Events order it: a buffer is refilled only after the adjoint
+    // steps that read it (freed), and read only after its refill (ready).
+    const size_t buf_bytes = (size_t)w.C * w.plane_bytes;
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t setup = nullptr, done2 = nullptr, ready[2] = {}, freed[2] = {};
+    auto release = [&]() {
+      for (int b = 0; b < 2; ++b) {
+        if (ready[b]) cudaEventDestroy(ready[b]);
+        if (freed[b]) cudaEventDestroy(freed[b]);
+      }
+      if (setup) cudaEventDestroy(setup);
+      if (done2) cudaEventDestroy(done2);
+      if (s2) cudaStreamDestroy(s2);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&setup, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done2, cudaEventDisableTiming);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+      e = cudaEventCreateWithFlags(&ready[b], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&freed[b], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+      release();
+      return cuda_fail(e, "adjoint: streams");
+    }
+    // the halo of every stash slot of both buffers: the fixed boundary (never rewritten)
+    for (int k = 0; k < 2 * w.C; ++k)
       CK(cudaMemcpyAsync(stash + (size_t)k * w.plane_bytes, ws + w.off_cp, w.plane_bytes, cudaMemcpyDeviceToDevice,
                          s),
          "adjoint: stash");
-    for (int j = w.ncp - 1; j >= 0; --j) {
-      const int t0 = j * w.C;
-      const int c = std::min(w.C, d->timestep - t0);
-      if (c <= 0) continue;
-      // recompute u_{t0} .. u_{t0+c-1} into the stash, one launch per step
-      CK(cudaMemcpyAsync(stash, ws + w.off_cp + (size_t)j * w.plane_bytes, w.plane_bytes, cudaMemcpyDeviceToDevice,
-                         s),
-         "adjoint: restore");
-      for (int k = 1; k < c; ++k)
-        if ((st = launch_block(d, L, coef.data(), div, eps, 0, 1, stash + (size_t)(k - 1) * w.plane_bytes,
-                               stash + (size_t)k * w.plane_bytes, s, err)) != GBS_OK)
-          return st;
+    cudaEventRecord(setup, s);
+    cudaStreamWaitEvent(s2, setup, 0);
+    // recompute u_{t0} .. u_{t0+c-1} of chunk j into buffer j % 2 on s2
+    auto recompute = [&](int j) -> gbs_status {
+      const int b = j & 1;
+      char *buf = stash + (size_t)b * buf_bytes;
+      const int c = std::min(w.C, d->timestep - j * w.C);
+      cudaStreamWaitEvent(s2, freed[b], 0);  // no-op before the buffer's first use
+      cudaError_t ce = cudaMemcpyAsync(buf, ws + w.off_cp + (size_t)j * w.plane_bytes, w.plane_bytes,
+                                       cudaMemcpyDeviceToDevice, s2);
+      if (ce != cudaSuccess) return cuda_fail(ce, "adjoint: restore");
+      for (int k = 1; k < c; ++k) {
+        gbs_status r = launch_block(d, L, coef.data(), div, eps, 0, 1, buf + (size_t)(k - 1) * w.plane_bytes,
+                                    buf + (size_t)k * w.plane_bytes, s2, err);
+        if (r != GBS_OK) return r;
+      }
+      cudaEventRecord(ready[b], s2);
+      return GBS_OK;
+    };
+    st = recompute(w.ncp - 1);
+    for (int j = w.ncp - 1; j >= 0 && st == GBS_OK; --j) {
+      const int b = j & 1;
+      const int c = std::min(w.C, d->timestep - j * w.C);
+      if (j > 0 && (st = recompute(j - 1)) != GBS_OK) break;  // overlaps the steps below
+      cudaStreamWaitEvent(s, ready[b], 0);
       // lam_{t+1} -> lam_t for t = t0+c-1 .. t0
-      for (int k = c - 1; k >= 0; --k)
-        if ((st = step(stash + (size_t)k * w.plane_bytes)) != GBS_OK) return st;
+      char *buf = stash + (size_t)b * buf_bytes;
+      for (int k = c - 1; k >= 0 && st == GBS_OK; --k) st = step(buf + (size_t)k * w.plane_bytes);
+      cudaEventRecord(freed[b], s);
     }
+    // every piece of s2's work is ordered before s (the last ready event); join anyway
+    cudaEventRecord(done2, s2);
+    cudaStreamWaitEvent(s, done2, 0);
+    release();
+    if (st != GBS_OK) return st;
   }
   if (d->dtype == GBS_F64)
     combine_kernel<double><<<blocks, kAdjThreads, 0, s>>>((const double *)lam[cur], (const double *)hg,

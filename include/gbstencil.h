@@ -249,8 +249,9 @@ gbs_status gbs_batch_run_noalloc(const gbs_batch_grid *grids, int ngrids, int fp
  * coefficients as the source writes them, before a divisor; stencils of at
  * most 32 terms; gradient2d: one value, for its numerator). gradient2d uses
  * its linearised update. Each chunk's
- * states are recomputed from its checkpoint. Both calls are asynchronous on
- * `stream`. */
+ * states are recomputed from its checkpoint, into one of two stash buffers
+ * on an internal second stream while the previous chunk's adjoint steps run
+ * on `stream`. Both calls are asynchronous on `stream`. */
 gbs_status gbs_adjoint_workspace(const gbs_desc *d, int checkpoint_every, size_t *bytes);
 gbs_status gbs_adjoint_forward(const gbs_desc *d, void *dev_A, int checkpoint_every, void *workspace,
                                void *stream);

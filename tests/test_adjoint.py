@@ -208,9 +208,10 @@ def test_adjoint_argument_checks():
                                                ("gradient2d", np.float64, 4096, 512, 32),
                                                ("j3d27pt", np.float32, 64, 20, 6)])
 def test_adjoint_workspace_size(name, dtype, n, T, C):
-    """Checkpoints (ceil(T/C) planes) + stash (C) + two lam planes + the
-    halo-gradient plane (+ q and sum-of-differences planes for gradient2d)
-    + the partial-sum table, as the C ABI reports it (host arithmetic only)."""
+    """Checkpoints (ceil(T/C) planes) + two stash buffers (2C) + two lam
+    planes + the halo-gradient plane (+ q and sum-of-differences planes for
+    gradient2d) + the partial-sum table, as the C ABI reports it (host
+    arithmetic only)."""
     from gbstencil import capi
     d, _ = capi.make_desc(name, dtype, n, T, "fma")
     nbytes = ctypes.c_size_t(0)
@@ -218,7 +219,7 @@ def test_adjoint_workspace_size(name, dtype, n, T, C):
     L = capi.layout(d)
     plane = L.plane * np.dtype(dtype).itemsize
     s = capi.info(name)
-    planes = -(-T // C) + C + 3 + (2 if s["kind"] == "gradient" else 0)
+    planes = -(-T // C) + 2 * C + 3 + (2 if s["kind"] == "gradient" else 0)
     assert nbytes.value >= planes * plane
     assert nbytes.value - planes * plane < 64 * 1024 * 1024   # the partial table and slack only
     # the 16 GB budget of the gradient2d configuration holds
