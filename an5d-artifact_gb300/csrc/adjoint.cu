@@ -801,19 +801,18 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
   CK(cudaMemsetAsync(part, 0, (size_t)w.nblocks * w.nt * sizeof(double), s), "adjoint: memset");
   int cur = 0;
   // one adjoint step lam[cur] (= lam_{t+1}) -> lam[cur ^ 1] (= lam_t) on state u_t
-  cudaStream_t sa = s;  // the stream the adjoint steps run on
   auto step = [&](const char *u) -> gbs_status {
     if (gradient) {
       CK(K.grad(g, u, ws + w.off_q, ws + w.off_sd, lam[cur], lam[cur ^ 1], hg, part, coef[0], eps,
-                dev_coef_grad != nullptr, sa),
+                dev_coef_grad != nullptr, s),
          "adjoint: gradient2d step");
     } else if (g.dim == 2 && sd->nterms <= kMaxCoefGrad) {
-      CK(K.fused2d(g, lam[cur], u, lam[cur ^ 1], hg, part, coef, div, dev_coef_grad != nullptr, sa),
+      CK(K.fused2d(g, lam[cur], u, lam[cur ^ 1], hg, part, coef, div, dev_coef_grad != nullptr, s),
          "adjoint: fused 2-D step");
     } else {
-      CK(K.halo(g, lam[cur], hg, coef, div, sa), "adjoint: halo");
-      if (dev_coef_grad) CK(K.coef(g, lam[cur], u, part, div, sa), "adjoint: coefficients");
-      gbs_status r = launch_block(&dT, L, coefT.data(), div, eps, 0, 1, lam[cur], lam[cur ^ 1], sa, err);
+      CK(K.halo(g, lam[cur], hg, coef, div, s), "adjoint: halo");
+      if (dev_coef_grad) CK(K.coef(g, lam[cur], u, part, div, s), "adjoint: coefficients");
+      gbs_status r = launch_block(&dT, L, coefT.data(), div, eps, 0, 1, lam[cur], lam[cur ^ 1], s, err);
       if (r != GBS_OK) return r;
     }
     cur ^= 1;
@@ -830,28 +829,19 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
     // buffer. Events order it: a buffer is refilled only after the adjoint
     // steps that read it (freed), and read only after its refill (ready).
     const size_t buf_bytes = (size_t)w.C * w.plane_bytes;
-    // The adjoint steps (the critical path) run on an internal stream of the
-    // highest priority, the recompute on one of the lowest, so that the
-    // recompute fills the SMs the steps leave free; both join `s` at the end.
-    cudaStream_t s1 = nullptr, s2 = nullptr;
-    cudaEvent_t setup = nullptr, done1 = nullptr, done2 = nullptr, ready[2] = {}, freed[2] = {};
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t setup = nullptr, done2 = nullptr, ready[2] = {}, freed[2] = {};
     auto release = [&]() {
       for (int b = 0; b < 2; ++b) {
         if (ready[b]) cudaEventDestroy(ready[b]);
         if (freed[b]) cudaEventDestroy(freed[b]);
       }
       if (setup) cudaEventDestroy(setup);
-      if (done1) cudaEventDestroy(done1);
       if (done2) cudaEventDestroy(done2);
-      if (s1) cudaStreamDestroy(s1);
       if (s2) cudaStreamDestroy(s2);
     };
-    int prio_low = 0, prio_high = 0;
-    cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s1, cudaStreamNonBlocking, prio_high);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s2, cudaStreamNonBlocking, prio_low);
+    cudaError_t e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&setup, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done1, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done2, cudaEventDisableTiming);
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
       e = cudaEventCreateWithFlags(&ready[b], cudaEventDisableTiming);
@@ -867,9 +857,7 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
                          s),
          "adjoint: stash");
     cudaEventRecord(setup, s);
-    cudaStreamWaitEvent(s1, setup, 0);
     cudaStreamWaitEvent(s2, setup, 0);
-    sa = s1;
     // recompute u_{t0} .. u_{t0+c-1} of chunk j into buffer j % 2 on s2
     auto recompute = [&](int j) -> gbs_status {
       const int b = j & 1;
@@ -892,18 +880,15 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
       const int b = j & 1;
       const int c = std::min(w.C, d->timestep - j * w.C);
       if (j > 0 && (st = recompute(j - 1)) != GBS_OK) break;  // overlaps the steps below
-      cudaStreamWaitEvent(s1, ready[b], 0);
+      cudaStreamWaitEvent(s, ready[b], 0);
       // lam_{t+1} -> lam_t for t = t0+c-1 .. t0
       char *buf = stash + (size_t)b * buf_bytes;
       for (int k = c - 1; k >= 0 && st == GBS_OK; --k) st = step(buf + (size_t)k * w.plane_bytes);
-      cudaEventRecord(freed[b], s1);
+      cudaEventRecord(freed[b], s);
     }
-    // join both streams back into the caller's stream
-    cudaEventRecord(done1, s1);
+    // every piece of s2's work is ordered before s (the last ready event); join anyway
     cudaEventRecord(done2, s2);
-    cudaStreamWaitEvent(s, done1, 0);
     cudaStreamWaitEvent(s, done2, 0);
-    sa = s;
     release();
     if (st != GBS_OK) return st;
   }
