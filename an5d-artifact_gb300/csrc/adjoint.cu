@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cstring>
 #include <vector>
 
@@ -609,6 +610,22 @@ int one_wave(K kernel) {
   return std::max(1, std::min(kCoefBlocks, nb * sms));
 }
 
+// one_wave(kernel) for the current device, computed once per device ordinal
+// (a process may drive GPUs with different SM counts)
+template <class K>
+int wave_cached(K kernel) {
+  static std::mutex mu;
+  static int cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    (void)cudaGetLastError();
+    return one_wave(kernel);
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (cache[dev] == 0) cache[dev] = one_wave(kernel);
+  return cache[dev];
+}
+
 // one thread per halo cell of the interior rows, one warp per segment of an all-halo row
 unsigned halo_grid(const AdjGeom &g) {
   const HaloPlan h = halo_plan(g);
@@ -643,8 +660,8 @@ cudaError_t run_fused2d(const AdjGeom &g, const void *lam, const void *u, void *
     const HaloPlan hp = halo_plan(g);
     const long long halo_threads = hp.na + hp.rows_b * hp.nseg * 32;
     const unsigned halo_blocks = (unsigned)((halo_threads + kAdjThreads - 1) / kAdjThreads);
-    static const int wave_c = one_wave(adj2d_kernel<ST, T, true>);
-    static const int wave_n = one_wave(adj2d_kernel<ST, T, false>);
+    const int wave_c = wave_cached(adj2d_kernel<ST, T, true>);
+    const int wave_n = wave_cached(adj2d_kernel<ST, T, false>);
     if (want_coef)
       adj2d_kernel<ST, T, true><<<wave_c + halo_blocks, kAdjThreads, 0, s>>>(
           g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
@@ -663,7 +680,7 @@ cudaError_t run_coef(const AdjGeom &g, const void *lam, const void *u, double *p
     return cudaErrorInvalidValue;
   } else {
     const double dv = ST::kHasDiv ? div : 1.0;
-    static const int wave = one_wave(coef_kernel<ST, T>);
+    const int wave = wave_cached(coef_kernel<ST, T>);
     coef_kernel<ST, T><<<wave, kAdjThreads, 0, s>>>(g, static_cast<const T *>(lam), static_cast<const T *>(u), part,
                                                     (T)(1.0 / dv));
     return cudaGetLastError();
@@ -852,10 +869,14 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
       return cuda_fail(e, "adjoint: streams");
     }
     // the halo of every stash slot of both buffers: the fixed boundary (never rewritten)
-    for (int k = 0; k < 2 * w.C; ++k)
-      CK(cudaMemcpyAsync(stash + (size_t)k * w.plane_bytes, ws + w.off_cp, w.plane_bytes, cudaMemcpyDeviceToDevice,
-                         s),
-         "adjoint: stash");
+    for (int k = 0; k < 2 * w.C; ++k) {
+      e = cudaMemcpyAsync(stash + (size_t)k * w.plane_bytes, ws + w.off_cp, w.plane_bytes, cudaMemcpyDeviceToDevice,
+                          s);
+      if (e != cudaSuccess) {
+        release();
+        return cuda_fail(e, "adjoint: stash");
+      }
+    }
     cudaEventRecord(setup, s);
     cudaStreamWaitEvent(s2, setup, 0);
     // recompute u_{t0} .. u_{t0+c-1} of chunk j into buffer j % 2 on s2

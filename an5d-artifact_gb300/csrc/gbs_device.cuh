@@ -105,19 +105,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
       : "memory");
 }
 
-// ---- tensor-map (TMA tiled) loads -------------------------------------------
-__device__ __forceinline__ void tma_load_4d(void *dst, const void *tmap, int c0, int c1, int c2,
-                                            int c3, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
-      "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void prefetch_tmap(const void *tmap) {
-  asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
-}
-
 // ---- vectors of V elements (16 bytes) ----------------------------------------
 template <typename T, int V> struct alignas(16) Vec { T v[V]; };
 

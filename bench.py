@@ -65,11 +65,13 @@ BATCH_MIX = ["star2d1r", "star2d2r", "star2d3r", "star2d4r", "box2d1r", "box2d2r
 
 # DRAM bytes (read + write) per interior cell per launch of the dominant
 # kernels, from ncu captures of small cases (dram__bytes_read.sum +
-# dram__bytes_write.sum over the interior cells of that case); the summaries
-# under profiles/ give the captures. Keyed by (stencil, dtype, bt).
+# dram__bytes_write.sum over the interior cells of that case), scaled to a
+# full launch by its interior cells (a launch reads and writes each plane
+# once, so traffic grows in proportion). Keyed by (stencil, dtype, bt); the
+# value names the capture, whose summary is under profiles/.
 NCU_DRAM_BYTES_PER_CELL = {
-    ("box3d1r", "float64", 1): 15.74,   # 256^3 capture: 171.3 MB read + 92.8 MB written
-    ("star3d2r", "float32", 1): 8.20,   # 320^3 capture: 180.2 MB read + 88.4 MB written
+    ("box3d1r", "float64", 1): (15.74, "profiles/stencil3d_rows_box3d1r_f64_n256.md (256^3 capture)"),
+    ("star3d2r", "float32", 1): (8.20, "profiles/stencil3d_rows_star3d2r_f32_n320.md (320^3 capture)"),
 }
 
 
@@ -252,48 +254,100 @@ def run_ours(args, rank, world):
         for g, h, c, (_, _, _, T) in zip(grids, hosts, coefs, work):
             d, keep = capi.make_desc(g.name, g.dtype, g.n, T, args.fp_mode, coef=c)
             capi.run_host(d, h.numpy())
+    e2e_samples = []
     if not args.no_e2e:
         e2e_step()  # allocates gbs_run's device buffer once
         torch.cuda.synchronize()
-        e2e_steps = max(1, min(args.steps, 2))
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
+        for _ in range(max(1, min(args.steps, args.e2e_steps))):
+            t0 = time.perf_counter()
             e2e_step()
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+            e2e_samples.append(round((time.perf_counter() - t0) * 1e3, 3))
+        e2e_ms = statistics.median(e2e_samples)
     h2d = sum(int(h.numel()) * h.element_size() for h in hosts)
     d2h = h2d
+    del hosts
 
-    # roofline of the dominant grid (largest device time)
+    # each grid's kernel (the same degree and tiling) on a reduced number of
+    # steps, against the CPU oracle in the same precision
+    errs, err_note = [None] * len(grids), None
+    if not args.no_check:
+        import pyoracle as po
+        for i, (g, c, p) in enumerate(zip(grids, coefs, plans)):
+            Tc = 2 * p.bt if p.bt > 1 else 4
+            g.fill_uniform(seed=20250101 + i)
+            A = g.download()
+            g.run(Tc, args.fp_mode, p.bt, 0, coef=c)
+            capi.sync(stream.cuda_stream)
+            got = g.download()
+            po.run(g.name, A, g.n, Tc, coef=c)
+            errs[i] = float(f"{po.normwise_error(got, A, Tc):.3e}")
+            del A, got
+        err_note = ("max_err_vs_oracle: normwise max|gpu-cpu|/max|cpu| over plane T%2 after T = 2*bt steps "
+                    "(4 when bt = 1) of the timed kernel at the full grid size, against the CPU oracle in the "
+                    "same precision; bound 1e-5 (float), 1e-12 (double)")
+
+    # roofline of each grid: Roofline(bt) = min(B_HBM*bt/(2S), P_FP/FPP) cell
+    # updates per second; the binding roof is the smaller term
     hbm, peak_kind = load_peaks()
+    fp_peak = {np.dtype(np.float32): capi.measure_fp_peak(np.float32),
+               np.dtype(np.float64): capi.measure_fp_peak(np.float64)}
+    per = []
+    for i, (nm, d_, n_, T_) in enumerate(work):
+        ms = per_grid_ms[i] / args.steps
+        gc = int(np.prod(grids[i].n)) * T_ / (ms * 1e-3) / 1e9
+        s_ = capi.info(nm)
+        Sb = np.dtype(d_).itemsize
+        bt = plans[i].bt
+        roof_hbm = hbm * 1e9 * bt / (2 * Sb) / 1e9
+        roof_fp = fp_peak[np.dtype(d_)] * 1e9 / s_["fpp"] / 1e9
+        roof = min(roof_hbm, roof_fp)
+        roof1 = min(hbm * 1e9 / (2 * Sb) / 1e9, roof_fp)
+        per.append({"stencil": nm, "dtype": np.dtype(d_).name, "n": n_, "T": T_, "bt": bt,
+                    "launches": plans[i].launches, "ms": round(ms, 4), "gcells_s": round(gc, 2),
+                    "bound": ("hbm" if roof_hbm <= roof_fp else ("fp64" if Sb == 8 else "fp32")),
+                    "roofline_gcells_s": round(roof, 1), "frac_roofline": round(gc / roof, 4),
+                    "roofline_bt1_gcells_s": round(roof1, 1), "max_err_vs_oracle": errs[i]})
+
+    # the dominant kernel (largest device time), against its binding roof
     gi = int(np.argmax(per_grid_ms))
     name, dt, n, T = work[gi]
     p = plans[gi]
     S = np.dtype(dt).itemsize
     ncell = int(np.prod(grids[gi].n))
     launch_ms = per_grid_ms[gi] / args.steps / max(1, p.launches)
-    alg_bytes = 2 * S * ncell  # each launch reads and writes every cell once
-    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
-    fp_peak = {np.dtype(np.float32): capi.measure_fp_peak(np.float32),
-               np.dtype(np.float64): capi.measure_fp_peak(np.float64)}
+    # algorithmic work per launch: each cell read and written once (bytes),
+    # fpp flops per cell update, bt updates per cell (flops)
+    alg_bytes = 2 * S * ncell
+    hbm_achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     fpp = capi.info(name)["fpp"]
-    # FP rate of the dominant kernel: algorithmic flops (fpp per cell update,
-    # bt updates per cell per launch) over the launch time
     fp_achieved = fpp * p.bt * ncell / (launch_ms * 1e-3) / 1e9
     per_cell = NCU_DRAM_BYTES_PER_CELL.get((name, np.dtype(dt).name, p.bt))
-    traffic = None if per_cell is None else int(per_cell * ncell)
-    per = []
+    traffic = None if per_cell is None else int(per_cell[0] * ncell)
+    hbm_block = {"bound": "hbm", "achieved": round(hbm_achieved, 1), "peak": hbm, "unit": "GB/s",
+                 "frac": round(hbm_achieved / hbm, 4), "traffic": traffic,
+                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s"}
+    fp_block = {"bound": "fp64" if S == 8 else "fp32", "achieved": round(fp_achieved, 1),
+                "peak": round(fp_peak[np.dtype(dt)], 1), "unit": "GFLOP/s",
+                "frac": round(fp_achieved / fp_peak[np.dtype(dt)], 4), "traffic": traffic,
+                "flops_per_cell_update": fpp,
+                "peak_source": "measured on this GPU by gbs_measure_fp_peak (an FMA loop, 2 flops per FMA); "
+                               "MEASURED_PEAKS.json has no FP32/FP64 figure"}
+    binding = fp_block if per[gi]["bound"] != "hbm" else hbm_block
+    roofline = dict(binding)
+    roofline["kernel"] = f"{name} {np.dtype(dt).name} bt={p.bt}, {p.launches} launches of {ncell} cells"
+    roofline["traffic_source"] = (f"dram__bytes_read.sum + dram__bytes_write.sum per interior cell from "
+                                  f"{per_cell[1]}, times the cells of one launch" if per_cell else
+                                  "no capture of this kernel")
+    roofline["secondary"] = hbm_block if binding is fp_block else fp_block
+    # the aggregate split by element type (the same timed runs)
+    by_dtype = {}
     for i, (nm, d_, n_, T_) in enumerate(work):
-        ms = per_grid_ms[i] / args.steps
-        gc = int(np.prod(grids[i].n)) * T_ / (ms * 1e-3) / 1e9
-        s = capi.info(nm)
-        Sb = np.dtype(d_).itemsize
-        bt = plans[i].bt
-        roof = min(hbm * 1e9 * bt / (2 * Sb), fp_peak[np.dtype(d_)] * 1e9 / s["fpp"]) / 1e9
-        roof1 = min(hbm * 1e9 / (2 * Sb), fp_peak[np.dtype(d_)] * 1e9 / s["fpp"]) / 1e9
-        per.append({"stencil": nm, "dtype": np.dtype(d_).name, "n": n_, "T": T_, "bt": bt,
-                    "launches": plans[i].launches, "ms": round(ms, 4), "gcells_s": round(gc, 2),
-                    "roofline_gcells_s": round(roof, 1), "frac_roofline": round(gc / roof, 4),
-                    "roofline_bt1_gcells_s": round(roof1, 1)})
+        k = np.dtype(d_).name
+        c, m = by_dtype.get(k, (0, 0.0))
+        by_dtype[k] = (c + int(np.prod(grids[i].n)) * T_, m + per_grid_ms[i] / args.steps)
+    value_by_dtype = {k: round(c / (m * 1e-3) / 1e9, 3) for k, (c, m) in by_dtype.items()}
+    total_ms = sum(m for _, m in by_dtype.values())
+    time_share = {k: round(m / total_ms, 4) for k, (c, m) in by_dtype.items()}
     launches = sum(p.launches for p in plans) * args.steps
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world,
@@ -304,17 +358,14 @@ def run_ours(args, rank, world):
         "config": {"workload": args.workload, "grids": [f"{w[0]} {np.dtype(w[1]).name} {w[2]}^{capi.info(w[0])['dim']} T={w[3]}" for w in work],
                    "fp_mode": args.fp_mode, "l2": "flushed between timed steps (512 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
+        "value_by_dtype": value_by_dtype,
+        "time_share_by_dtype": time_share,
         "per_stencil": per,
         "e2e": None if args.no_e2e else {
             "value": round(cells * world / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GCells/s",
-            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": traffic,
-                     "kernel": f"{name} {np.dtype(dt).name} bt={p.bt}, {p.launches} launches of {ncell} cells",
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                     "fp": {"achieved_gflops": round(fp_achieved, 1), "peak_gflops": round(fp_peak[np.dtype(dt)], 1),
-                            "frac": round(fp_achieved / fp_peak[np.dtype(dt)], 4),
-                            "flops_per_cell_update": fpp, "peak_source": "gbs_measure_fp_peak (FMA loop)"}},
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "samples_ms": e2e_samples},
+        "err_check": err_note,
+        "roofline": roofline,
         "fp_peak_gflops": {k.name: round(v, 1) for k, v in fp_peak.items()},
         "clocks": clk.summary(),
         "gpu_launches": launches,
@@ -371,10 +422,10 @@ def run_reference(args, rank, world):
     threads = po.max_threads()
     vals = []
     for _ in range(args.warmup):
-        cpu_sample(work, budget_s=2.0)
+        cpu_sample(work, budget_s=args.cpu_budget or 2.0)
     sample = ""
     for _ in range(args.steps):
-        v, sample = cpu_sample(work, budget_s=max(2.0, 60.0 / max(1, args.steps)))
+        v, sample = cpu_sample(work, budget_s=args.cpu_budget or max(2.0, 60.0 / max(1, args.steps)))
         vals.append(v)
     value = statistics.median(vals)
     return {
@@ -645,7 +696,23 @@ def run_adjoint(args, rank, world):
     }
 
 
-def main():
+def launch_ranks(argv, n):
+    """Runs this script as n ranks (one process per GPU) under
+    torch.distributed.run on this node and returns its exit status; rank 0
+    prints the line."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py")]
+    # the ranks' arguments travel in the environment: torch.distributed.run
+    # would read abbreviations such as --n as its own options
+    env = dict(os.environ, GBS_BENCH_ARGV=json.dumps(list(argv)))
+    return subprocess.run(cmd, env=env).returncode
+
+
+def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -662,17 +729,34 @@ def main():
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
     ap.add_argument("--batch-mode", default="streams", choices=["persistent", "layered", "streams"],
                     help="batched workload: scheduling of the work items")
-    args = ap.parse_args()
+    ap.add_argument("--e2e-steps", type=int, default=3, help="timed host-buffer samples (at most --steps)")
+    ap.add_argument("--no-check", action="store_true", help="skip the per-grid error check against the oracle")
+    ap.add_argument("--cpu-budget", type=float, default=0.0,
+                    help="seconds of CPU work per CPU-baseline sample (0: the default)")
+    ap.add_argument("--dist-backend", default="nccl", help="process-group backend of N > 1 ranks")
+    if argv is None and os.environ.get("GBS_BENCH_ARGV") and "WORLD_SIZE" in os.environ:
+        argv = json.loads(os.environ["GBS_BENCH_ARGV"])
+    args = ap.parse_args(argv)
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        # one process per GPU: re-run this script as args.gpus ranks
+        return launch_ranks(sys.argv[1:] if argv is None else list(argv), args.gpus)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if world != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}", file=sys.stderr)
+        return 2
     if args.impl == "reference":
         if rank != 0:
-            return
+            return 0
         print(json.dumps(run_reference(args, rank, world)))
-        return
+        return 0
     if world > 1:
         import torch
-        torch.distributed.init_process_group("nccl")
+        if args.dist_backend == "nccl" and int(os.environ.get("LOCAL_RANK", 0)) >= torch.cuda.device_count():
+            print(f"bench.py: rank {rank} has no GPU of its own ({torch.cuda.device_count()} visible)",
+                  file=sys.stderr)
+            return 2
+        torch.distributed.init_process_group(args.dist_backend)
     if args.workload == "batched":
         line = run_batched(args, rank, world)
     elif args.workload == "adjoint":
@@ -682,14 +766,15 @@ def main():
     if rank == 0:
         if not args.no_cpu:
             import pyoracle as po
-            v, sample = cpu_sample(cpu_work(args))
+            v, sample = cpu_sample(cpu_work(args), budget_s=args.cpu_budget or 12.0)
             line["cpu_baseline"] = {"value": round(v, 4), "unit": "GCells/s", "cores": po.max_threads(),
                                     "kind": "port", "sample": sample}
         print(json.dumps(line))
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()
+    return 0
 
 
 if __name__ == "__main__":
-    main()
+    sys.exit(main())

@@ -98,6 +98,38 @@ def test_adjoint_matches_reference(name, dtype, n, T, C):
     assert _rel(gc, ref_gc) <= tol, name
 
 
+WIDE_CASES = [
+    # rows wider than one lane segment (32 lanes x 16 bytes: 128 float or 64
+    # double columns), so that in-row neighbours cross segments and warps
+    # loop over several units; radius above the vector width (R > V)
+    ("j2d5pt", np.float32, 300, 6, 4, True),
+    ("j2d5pt", np.float32, 300, 6, 4, False),
+    ("star2d3r", np.float64, 200, 5, 2, True),
+    ("star2d3r", np.float64, 200, 5, 2, False),
+    ("star2d4r", np.float64, 140, 4, 3, True),
+    ("box2d3r", np.float32, 170, 4, 2, False),
+    ("box2d4r", np.float32, 150, 4, 2, False),
+    ("box2d4r", np.float64, 150, 4, 3, False),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,dtype,n,T,C,want_coef", WIDE_CASES,
+                         ids=lambda v: getattr(v, "__name__", str(v)))
+def test_adjoint_matches_reference_wide_rows(name, dtype, n, T, C, want_coef):
+    u0, w = _inputs(name, n, 4)
+    u0 = u0.astype(dtype).astype(np.float64)
+    coef = ar.default_coef(name)
+    uT, gu, gc = _gpu_adjoint(name, dtype, u0, w, T, C, want_coef=want_coef)
+    ref_gu, ref_gc = ar.adjoint(name, u0, coef, T, w)
+    tol = 1e-4 if dtype == np.float32 else 1e-9
+    assert _rel(gu, ref_gu) <= tol, name
+    if want_coef:
+        assert _rel(gc, ref_gc) <= tol, name
+    else:
+        assert gc is None
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["j2d5pt", "gradient2d", "star3d1r"])
 def test_adjoint_directional_finite_difference(name):

@@ -47,3 +47,32 @@ def test_single_rank_is_the_standard_set():
     import bench
     assert bench.rank_specs(8, 0, 1) == bench.batched_specs(8)
     assert bench.max_over_ranks(3.5, 1) == 3.5
+
+
+def _bench(args, env_extra=None, drop=("WORLD_SIZE", "RANK", "LOCAL_RANK")):
+    import subprocess
+    env = {k: v for k, v in os.environ.items() if k not in drop}
+    env.update(env_extra or {})
+    return subprocess.run([sys.executable, str(ROOT / "bench.py")] + args, capture_output=True, text=True,
+                          timeout=600, env=env)
+
+
+SMALL = ["--impl", "reference", "--workload", "star2d1r", "--n", "128", "--T", "4", "--steps", "1",
+         "--warmup", "0", "--cpu-budget", "0.2"]
+
+
+def test_gpus_flag_launches_one_process_per_rank():
+    """bench.py --gpus 2 outside torchrun re-runs itself as two ranks under
+    torch.distributed.run (127.0.0.1); rank 0 alone prints the line."""
+    import json
+    r = _bench(["--gpus", "2"] + SMALL)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = json.loads(lines[0])
+    assert line["n_gpus"] == 2 and line["impl"] == "reference"
+
+
+def test_gpus_flag_never_silently_runs_fewer_ranks():
+    r = _bench(["--gpus", "2"] + SMALL, env_extra={"WORLD_SIZE": "1", "RANK": "0"})
+    assert r.returncode != 0 and "WORLD_SIZE" in r.stderr

@@ -10,7 +10,19 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-ARTIFACT = Path("/root/reference")
+
+
+def _artifact_dir() -> Path:
+    """The artifact's sources: AN5D_ARTIFACT_DIR, else the directory the
+    oracle's pin was last built from (oracle/_ref/artifact_dir)."""
+    import os
+    if os.environ.get("AN5D_ARTIFACT_DIR"):
+        return Path(os.environ["AN5D_ARTIFACT_DIR"])
+    rec = ROOT / "oracle" / "_ref" / "artifact_dir"
+    return Path(rec.read_text().strip()) if rec.exists() else ROOT / "missing-artifact"
+
+
+ARTIFACT = _artifact_dir()
 LIB = ROOT / "an5d-artifact_gb300" / "gbstencil" / "_lib"
 
 
