@@ -7,6 +7,7 @@
 // a launch sequence whose final plane is T%2 by construction, host-side
 // validation of every address range a launch touches, and status codes in
 // place of asserts.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -151,6 +152,46 @@ static void resolve_bt_sl(const gbs_desc *d, int *bt, int *sl) {
   *sl = d->sl > 0 ? d->sl : (tuned && tb == *bt ? ts : 0);
 }
 
+// ---------------------------------------------------------------------------
+// tensor maps (cuTensorMapEncodeTiled, reached through the runtime's driver
+// entry point so that the library needs no link against libcuda)
+// ---------------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled_fn() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    (void)cudaGetLastError();
+  });
+  return fn;
+}
+
+cudaError_t encode_plane_map(void *map, const void *plane, int esize, long long pitch, int d1, int d0, int bx,
+                             int by) {
+  EncodeTiledFn fn = encode_tiled_fn();
+  if (!fn) return cudaErrorNotSupported;
+  if (reinterpret_cast<uintptr_t>(plane) % 16 != 0 || (pitch * esize) % 16 != 0) return cudaErrorInvalidValue;
+  const cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)d1, (cuuint64_t)d0};
+  const cuuint64_t strides[2] = {(cuuint64_t)pitch * esize, (cuuint64_t)pitch * esize * (cuuint64_t)d1};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(static_cast<CUtensorMap *>(map),
+                        esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                        const_cast<void *>(plane), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 // Divisors for which the exhaustive self-test (every float input, see
 // gbs_check_division) shows the one-correction quotient equal to IEEE
 // division: the artifact's 118 and 159. The GPU test suite re-proves this.
@@ -228,21 +269,29 @@ long long resident_ctas_3d(int sid, int dtype, int fma, int b) {
   return (long long)c * sm_count();
 }
 
-// Tiles of 32 rows x one 32*V-column window; the number of stream blocks is
-// chosen to fill whole waves of resident CTAs while keeping the 2*b*r-plane
-// stream overlap small.
-int tile_rows_3d(int sid, int dtype, int fma, int b) {
+Tile3DShape tile_shape_3d(int sid, int dtype, int fma, int b) {
   const Picks &pk = picks(sid, dtype, fma);
-  return (b <= kMaxB && pk.tj3[b] > 0) ? pk.tj3[b] : 32;
+  Tile3DShape t{};
+  if (b >= 1 && b <= kMaxB && pk.tj3[b] > 0) {
+    t.tj = pk.tj3[b];
+    t.jout = pk.jout3[b];
+    t.wk = pk.wk3[b];
+    t.tile = pk.tile3[b];
+  }
+  return t;
 }
 
-Geometry3D geometry3d(const Layout &L, int b, int tj, int sl_req, long long resident) {
+// Tiles of the launcher's shape (rows x one 32*V-column window); the number
+// of stream blocks is chosen to fill whole waves of resident CTAs while
+// keeping the 2*b*r-plane stream overlap small.
+Geometry3D geometry3d(const Layout &L, int b, const Tile3DShape &ts, int sl_req, long long resident) {
   Geometry3D g{};
-  const int R = L.rad, V = L.V;
+  const int R = L.rad;
   g.b = b;
-  g.tj = tj;
-  g.jout = g.tj - 2 * b * R;
-  g.wk = ((32 * V - 2 * b * R - (V - 1)) / V) * V;
+  g.tj = ts.tj;
+  g.jout = ts.jout;
+  g.wk = ts.wk;
+  g.tile = ts.tile;
   const int ni = L.dims[0] - 2 * R, nj = L.dims[1] - 2 * R, nk = L.dims[2] - 2 * R;
   g.ntk = g.wk > 0 ? (nk + g.wk - 1) / g.wk : 1;
   g.ntj = g.jout > 0 ? (nj + g.jout - 1) / g.jout : 1;
@@ -270,10 +319,16 @@ Geometry3D geometry3d(const Layout &L, int b, int tj, int sl_req, long long resi
 
 gbs_status validate3d(const Layout &L, const Geometry3D &g) {
   const int R = L.rad, V = L.V, ROW = 32 * V;
+  if (g.tj <= 0) return fail(GBS_ERR_UNSUPPORTED, "no 3-D kernel of degree %d", g.b);
   if (g.jout <= 0 || g.wk <= 0)
     return fail(GBS_ERR_UNSUPPORTED, "fused degree %d leaves no output cells in a %d-row tile (r=%d)", g.b,
                 g.tj, R);
   if ((L.pitch * (long long)L.esize) % 16 != 0) return fail(GBS_ERR_INVALID, "internal: pitch alignment");
+  if ((L.shift + R) % V != 0) return fail(GBS_ERR_INVALID, "internal: first interior column not aligned");
+  if (g.wk % V != 0) return fail(GBS_ERR_INVALID, "internal: tile width not a whole number of vectors");
+  // the tile kernel's plane copies are tensor-map boxes: the hardware fills
+  // what lies outside the plane, and its halo loads are guarded per lane
+  if (g.tile) return GBS_OK;
   for (int t = 0; t < g.ntk; ++t) {
     const int cs = R + t * g.wk;
     const int ce = std::min(cs + g.wk, L.dims[2] - R);
@@ -424,7 +479,7 @@ gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, 
       cudaError_t e = pk.l2[b](a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");
     } else {
-      Geometry3D g = geometry3d(L, b, tile_rows_3d(d->stencil, d->dtype, fma, b), sl,
+      Geometry3D g = geometry3d(L, b, tile_shape_3d(d->stencil, d->dtype, fma, b), sl,
                                  resident_ctas_3d(d->stencil, d->dtype, fma, b));
       gbs_status st = validate3d(L, g);
       if (st != GBS_OK) return st;
@@ -529,7 +584,7 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
     const double cols = 32.0 * L.V, rows = g.sl + 2.0 * bt * L.rad;
     out->redundancy = (cols * rows) / ((double)g.wout * g.sl);
   } else {
-    Geometry3D g = geometry3d(L, bt, tile_rows_3d(d->stencil, d->dtype, fma, bt), sl,
+    Geometry3D g = geometry3d(L, bt, tile_shape_3d(d->stencil, d->dtype, fma, bt), sl,
                                  resident_ctas_3d(d->stencil, d->dtype, fma, bt));
     st = validate3d(L, g);
     if (st != GBS_OK) return st;
@@ -539,6 +594,7 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
     out->ctas = g.ntk * g.ntj * g.nblocks;
     out->valid_w = g.wk;
     out->redundancy = (32.0 * L.V * g.tj * (g.sl + 2.0 * bt * L.rad)) / ((double)g.wk * g.jout * g.sl);
+    out->bs1 = g.tj;
   }
   return GBS_OK;
 }

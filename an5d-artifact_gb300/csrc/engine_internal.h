@@ -29,9 +29,15 @@ struct Geometry2D {
 
 struct Geometry3D {
   int b, tj, jout, wk, ntk, ntj, nblocks, sl;
+  int tile;  // the tensor-map tile kernel (its copies are bounds-checked by the hardware)
 };
-Geometry3D geometry3d(const Layout &L, int b, int tj, int sl_req, long long resident_ctas);
-int tile_rows_3d(int sid, int dtype, int fma, int b);
+// Tile shape of the 3-D launcher of degree b: computed rows, valid rows and
+// valid columns per tile, and whether it is the tensor-map tile kernel.
+struct Tile3DShape {
+  int tj, jout, wk, tile;
+};
+Tile3DShape tile_shape_3d(int sid, int dtype, int fma, int b);
+Geometry3D geometry3d(const Layout &L, int b, const Tile3DShape &ts, int sl_req, long long resident_ctas);
 gbs_status validate3d(const Layout &L, const Geometry3D &g);
 long long resident_ctas_3d(int sid, int dtype, int fma, int b);
 

@@ -47,7 +47,17 @@ struct Picks {
   Occupancy2DFn o2[kMaxB + 1];
   Launch3DFn l3[kMaxB + 1];
   Occupancy3DFn o3[kMaxB + 1];
-  int tj3[kMaxB + 1];   // tile rows of the 3-D launcher
+  int tj3[kMaxB + 1];    // tile rows of the 3-D launcher
+  int jout3[kMaxB + 1];  // valid (output) rows of its tile
+  int wk3[kMaxB + 1];    // valid (output) columns of its tile
+  int tile3[kMaxB + 1];  // 1: the tensor-map tile kernel (no column window checks needed)
 };
+
+// Encodes the tensor map of one time plane of a 3-D grid for the tile kernel:
+// a {pitch, d1, d0}-element tensor at `plane` (16-byte aligned), rows of
+// pitch*esize bytes, copied in boxes of bx x by x 1 elements (zero fill
+// outside). `map` points at a CUtensorMap (64-byte aligned storage).
+cudaError_t encode_plane_map(void *map, const void *plane, int esize, long long pitch, int d1, int d0, int bx,
+                             int by);
 
 }  // namespace gbs

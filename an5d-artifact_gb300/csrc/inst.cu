@@ -27,13 +27,21 @@ constexpr size_t smem_pick(int b, std::integer_sequence<int, Bs...>) {
   return r;
 }
 template <int... Bs>
-constexpr int rows_pick(int b, std::integer_sequence<int, Bs...>) {
+constexpr int jout_pick(int b, std::integer_sequence<int, Bs...>) {
   int r = 0;
-  ((r = (Bs + 1 == b) ? tile_rows3d<S, T, Bs + 1, kFma>() : r), ...);
+  ((r = (Bs + 1 == b) ? tile_jout3d<S, T, Bs + 1, kFma>() : r), ...);
   return r;
 }
-constexpr size_t smem_bytes3d_b(int b) { return smem_pick(b, std::make_integer_sequence<int, 4>()); }
-constexpr int tile_rows_b(int b) { return rows_pick(b, std::make_integer_sequence<int, 4>()); }
+template <int... Bs>
+constexpr int wk_pick(int b, std::integer_sequence<int, Bs...>) {
+  int r = 0;
+  ((r = (Bs + 1 == b) ? tile_wk3d<S, T, Bs + 1, kFma>() : r), ...);
+  return r;
+}
+constexpr int kMax3D = 4;  // largest 3-D degree considered
+constexpr size_t smem_bytes3d_b(int b) { return smem_pick(b, std::make_integer_sequence<int, kMax3D>()); }
+constexpr int jout_b(int b) { return jout_pick(b, std::make_integer_sequence<int, kMax3D>()); }
+constexpr int wk_b(int b) { return wk_pick(b, std::make_integer_sequence<int, kMax3D>()); }
 
 // Exact mode spends two FP instructions per term, so its best degree is
 // lower; it keeps degrees up to 4. In 3-D a tile of 32 rows loses 2*b*r rows
@@ -49,8 +57,9 @@ constexpr int max_class() {
   }
   if (S::kRad >= 3) return 1;
   int b = sizeof(T) == 8 ? 2 : (S::kRad == 1 ? 4 : 3);
-  // the level rings must fit the 227 KB of shared memory a CTA may use
-  while (b > 1 && (smem_bytes3d_b(b) > 227u * 1024u || tile_rows_b(b) <= 2 * b * S::kRad)) --b;
+  // the level rings must fit the 227 KB of shared memory a CTA may use, and
+  // the tile must keep output rows and columns after the overlap
+  while (b > 1 && (smem_bytes3d_b(b) > 227u * 1024u || jout_b(b) <= 0 || wk_b(b) <= 0)) --b;
   return b;
 }
 
@@ -63,6 +72,9 @@ template <int B> void add(Picks &p) {
       p.l3[B] = &launch3d<S, T, B, kFma>;
       p.o3[B] = &occupancy3d<S, T, B, kFma>;
       p.tj3[B] = tile_rows3d<S, T, B, kFma>();
+      p.jout3[B] = tile_jout3d<S, T, B, kFma>();
+      p.wk3[B] = tile_wk3d<S, T, B, kFma>();
+      p.tile3[B] = use_tile3d<S, kFma>() ? 1 : 0;
     }
     p.maxb = B;
   }

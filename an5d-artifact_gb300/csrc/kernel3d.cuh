@@ -678,6 +678,12 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
   }
 }
 
+}  // namespace gbs
+
+#include "kernel3d_tile.cuh"
+
+namespace gbs {
+
 // rows per warp of the FMA variant: as many as the partial sums allow in
 // the 128 registers a 512-thread CTA may use
 template <class ST, typename T, int B>
@@ -695,34 +701,59 @@ constexpr int kNw3D = 16;
 
 constexpr int kTj3D = 32;
 
-// Tile rows of the launcher for (ST, T, B, FMA): the engine's planner sizes
-// tiles with it.
-// The multi-row variant serves FMA mode except for the large boxes, whose
-// hundreds of terms per row make its per-row unrolling too big to inline;
-// they (and exact mode) use the one-row kernel.
+// The tile kernel (tensor-map copies, exact output coverage) serves FMA mode
+// except for the large boxes, whose hundreds of terms per row make its
+// per-row unrolling too big to inline; they (and exact mode) use the
+// one-row kernel.
 template <class ST, bool FMA>
-constexpr bool use_rows3d() { return FMA && ST::kTerms <= 125; }
+constexpr bool use_tile3d() { return FMA && ST::kTerms <= 125; }
+
+// level-0 stages of the tile kernel: four, or three where four do not fit
+template <class ST, typename T, int B>
+constexpr int tile_stages3d() {
+  return Tile3<ST, T, B, kNw3D, rows_per_warp<ST, T, B>(), 4>::bytes() <= 227u * 1024u ? 4 : 3;
+}
+template <class ST, typename T, int B>
+using TileOf = Tile3<ST, T, B, kNw3D, rows_per_warp<ST, T, B>(), tile_stages3d<ST, T, B>()>;
 
 template <class ST, typename T, int B, bool FMA>
 constexpr int tile_rows3d() {
-  return use_rows3d<ST, FMA>() ? kNw3D * rows_per_warp<ST, T, B>() : kTj3D;
+  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B>::TJ : kTj3D;
+}
+
+// valid rows and columns per tile of the launcher for (ST, T, B, FMA)
+template <class ST, typename T, int B, bool FMA>
+constexpr int tile_jout3d() {
+  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B>::JOUT : kTj3D - 2 * B * ST::kRad;
+}
+template <class ST, typename T, int B, bool FMA>
+constexpr int tile_wk3d() {
+  constexpr int V = 16 / sizeof(T);
+  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B>::WK : (32 * V - 2 * B * ST::kRad - (V - 1)) / V * V;
 }
 
 template <class ST, typename T, int B, bool FMA>
 constexpr size_t smem_bytes3d() {
-  if constexpr (use_rows3d<ST, FMA>()) return Rows3<ST, T, B, kNw3D, rows_per_warp<ST, T, B>()>::bytes();
+  if constexpr (use_tile3d<ST, FMA>()) return TileOf<ST, T, B>::bytes();
   else return Smem3<ST, T, FMA>::bytes(kTj3D, B);
 }
 
 template <class ST, typename T, int B, bool FMA>
 auto kernel3d_ptr() {
-  if constexpr (use_rows3d<ST, FMA>()) return stencil3d_rows_kernel<ST, T, B, kNw3D, rows_per_warp<ST, T, B>()>;
-  else return stencil3d_kernel<ST, T, B, FMA, kTj3D>;
+  if constexpr (use_tile3d<ST, FMA>()) {
+    using G = TileOf<ST, T, B>;
+    return stencil3d_tile_kernel<ST, T, B, kNw3D, rows_per_warp<ST, T, B>(), G::NS>;
+  } else {
+    return stencil3d_kernel<ST, T, B, FMA, kTj3D>;
+  }
 }
 
 template <class ST, typename T, int B, bool FMA>
+constexpr int threads3d() { return use_tile3d<ST, FMA>() ? kNw3D * 32 : kTj3D * 32; }
+
+template <class ST, typename T, int B, bool FMA>
 cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {
-  constexpr int NT = use_rows3d<ST, FMA>() ? kNw3D * 32 : kTj3D * 32;
+  constexpr int NT = threads3d<ST, T, B, FMA>();
   auto kern = kernel3d_ptr<ST, T, B, FMA>();
   const size_t smem = smem_bytes3d<ST, T, B, FMA>();
   static bool attr_set = false;
@@ -734,34 +765,57 @@ cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {
     }
     attr_set = true;
   }
-  Params3D<T, ST::kTerms> p;
-  p.src = static_cast<const T *>(a.src);
-  p.dst = static_cast<T *>(a.dst);
-  p.err = a.err;
-  p.pitch = a.pitch;
-  p.d0 = a.d0;
-  p.d1 = a.d1;
-  p.d2 = a.d2;
-  p.shift = a.shift;
-  p.jout = a.jout;
-  p.wk = a.wk;
-  p.ntk = a.ntk;
-  p.ntj = a.ntj;
-  p.nblocks = a.nblocks;
-  p.sl = a.sl;
   const bool fold = FMA && ST::kHasDiv;  // the divisor is nonzero (checked by the planner)
-  for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = fold ? (T)(a.coef[t] / a.div) : (T)a.coef[t];
-  p.divmode = !ST::kHasDiv || fold ? 0 : (a.div_proven ? 2 : 1);
-  p.div = (T)a.div;
-  p.rdiv = div_reciprocal<T>(a.div);
   const long long grid = (long long)a.ntk * a.ntj * a.nblocks;
-  kern<<<(unsigned)grid, NT, smem, stream>>>(p);
+  if constexpr (use_tile3d<ST, FMA>()) {
+    using G = TileOf<ST, T, B>;
+    Params3T<T, ST::kTerms> p;
+    cudaError_t e = encode_plane_map(&p.tmap, a.src, (int)sizeof(T), a.pitch, a.d1, a.d0, G::BX, G::BY);
+    if (e != cudaSuccess) return e;
+    p.src = static_cast<const T *>(a.src);
+    p.dst = static_cast<T *>(a.dst);
+    p.err = a.err;
+    p.pitch = a.pitch;
+    p.d0 = a.d0;
+    p.d1 = a.d1;
+    p.d2 = a.d2;
+    p.shift = a.shift;
+    p.jout = a.jout;
+    p.wk = a.wk;
+    p.ntk = a.ntk;
+    p.ntj = a.ntj;
+    p.nblocks = a.nblocks;
+    p.sl = a.sl;
+    for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = fold ? (T)(a.coef[t] / a.div) : (T)a.coef[t];
+    kern<<<(unsigned)grid, NT, smem, stream>>>(p);
+  } else {
+    Params3D<T, ST::kTerms> p;
+    p.src = static_cast<const T *>(a.src);
+    p.dst = static_cast<T *>(a.dst);
+    p.err = a.err;
+    p.pitch = a.pitch;
+    p.d0 = a.d0;
+    p.d1 = a.d1;
+    p.d2 = a.d2;
+    p.shift = a.shift;
+    p.jout = a.jout;
+    p.wk = a.wk;
+    p.ntk = a.ntk;
+    p.ntj = a.ntj;
+    p.nblocks = a.nblocks;
+    p.sl = a.sl;
+    for (int t = 0; t < ST::kTerms; ++t) p.coef[t] = fold ? (T)(a.coef[t] / a.div) : (T)a.coef[t];
+    p.divmode = !ST::kHasDiv || fold ? 0 : (a.div_proven ? 2 : 1);
+    p.div = (T)a.div;
+    p.rdiv = div_reciprocal<T>(a.div);
+    kern<<<(unsigned)grid, NT, smem, stream>>>(p);
+  }
   return cudaGetLastError();
 }
 
 template <class ST, typename T, int B, bool FMA>
 int occupancy3d() {
-  constexpr int NT = use_rows3d<ST, FMA>() ? kNw3D * 32 : kTj3D * 32;
+  constexpr int NT = threads3d<ST, T, B, FMA>();
   auto kern = kernel3d_ptr<ST, T, B, FMA>();
   const size_t smem = smem_bytes3d<ST, T, B, FMA>();
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {

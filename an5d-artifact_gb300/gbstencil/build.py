@@ -105,8 +105,9 @@ def build(jobs: int | None = None, verbose: bool = False, regcap: int = 0) -> Pa
     us = units()
     if regcap > 0:
         us = [(n, s, f + [f"-DGBS_REGCAP={regcap}"]) for n, s, f in us]
-    # big-radius 3-D boxes first: they are the slowest units
-    us.sort(key=lambda u: 0 if "picks_1" in u[0] else 1)
+    # the slowest units first: the batched kernels (every 2-D stencil in one
+    # unit), then the big-radius 3-D boxes
+    us.sort(key=lambda u: 0 if u[0].startswith("batch_") else (1 if "picks_1" in u[0] else 2))
     changed = False
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         for name, did, log in ex.map(lambda u: compile_unit(u, verbose, build_dir), us):

@@ -56,6 +56,9 @@ WORKLOADS = {
     "suite3d": [("star3d2r", np.float32, 512, 1000), ("star3d2r", np.float64, 512, 1000),
                 ("box3d1r", np.float32, 512, 1000), ("box3d1r", np.float64, 512, 1000)],
     "star2d1r": [("star2d1r", np.float32, 4096, 100)],
+    # the fp32 3-D grids of the fused-degree sweep (use with --bt)
+    "sweep3d": [("star3d2r", np.float32, 512, 100), ("box3d1r", np.float32, 512, 100),
+                ("j3d27pt", np.float32, 512, 100)],
 }
 
 
@@ -204,7 +207,7 @@ def run_ours(args, rank, world):
         g = DeviceGrid(name, dt, n, device=dev)
         g.fill_uniform(seed=20250101 + i)
         c = random_coefficients(name, dt, 1000 + i)
-        d, keep = g.desc(T, args.fp_mode, 0, 0, coef=c)
+        d, keep = g.desc(T, args.fp_mode, args.bt, 0, coef=c)
         plans.append(capi.plan(d))
         grids.append(g)
         coefs.append(c)
@@ -214,7 +217,7 @@ def run_ours(args, rank, world):
 
     def step():
         for g, c, (_, _, _, T) in zip(grids, coefs, work):
-            g.run(T, args.fp_mode, 0, 0, coef=c)
+            g.run(T, args.fp_mode, args.bt, 0, coef=c)
 
     for _ in range(args.warmup):
         step()
@@ -232,7 +235,7 @@ def run_ours(args, rank, world):
             flush.fill_(1.0)
             for gi, (g, c, (_, _, _, T)) in enumerate(zip(grids, coefs, work)):
                 ev[gi][0].record(stream)
-                g.run(T, args.fp_mode, 0, 0, coef=c)
+                g.run(T, args.fp_mode, args.bt, 0, coef=c)
                 ev[gi][1].record(stream)
             torch.cuda.synchronize()
             for gi in range(len(grids)):
@@ -252,7 +255,7 @@ def run_ours(args, rank, world):
     def e2e_step():
         nonlocal h2d, d2h
         for g, h, c, (_, _, _, T) in zip(grids, hosts, coefs, work):
-            d, keep = capi.make_desc(g.name, g.dtype, g.n, T, args.fp_mode, coef=c)
+            d, keep = capi.make_desc(g.name, g.dtype, g.n, T, args.fp_mode, bt=args.bt, coef=c)
             capi.run_host(d, h.numpy())
     e2e_samples = []
     if not args.no_e2e:
@@ -486,7 +489,7 @@ def run_batched(args, rank, world):
     # the same work as per-grid plain launches, one grid after another
     def plain():
         for g, T, c in entries:
-            g.run(T, args.fp_mode, 0, 0, coef=c)
+            g.run(T, args.fp_mode, args.bt, 0, coef=c)
     plain()
     capi.sync(stream.cuda_stream)
     torch.cuda.synchronize()
@@ -725,6 +728,7 @@ def main(argv=None):
     ap.add_argument("--only", default="", help="grids of the workload to keep, e.g. box3d1r:float64")
     ap.add_argument("--n", type=int, default=0, help="interior side length override")
     ap.add_argument("--T", type=int, default=0, help="timestep override")
+    ap.add_argument("--bt", type=int, default=0, help="fused degree of every grid (0: the tuned one)")
     ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
     ap.add_argument("--batch-mode", default="streams", choices=["persistent", "layered", "streams"],

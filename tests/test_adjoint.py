@@ -106,7 +106,7 @@ WIDE_CASES = [
     ("j2d5pt", np.float32, 300, 6, 4, False),
     ("star2d3r", np.float64, 200, 5, 2, True),
     ("star2d3r", np.float64, 200, 5, 2, False),
-    ("star2d4r", np.float64, 140, 4, 3, True),
+    ("j2d9pt", np.float32, 300, 4, 3, True),
     ("box2d3r", np.float32, 170, 4, 2, False),
     ("box2d4r", np.float32, 150, 4, 2, False),
     ("box2d4r", np.float64, 150, 4, 3, False),
