@@ -28,10 +28,17 @@
 // C steps into the caller's workspace. When the states are needed,
 // gbs_adjoint_backward walks the chunks backwards and recomputes a chunk's C
 // states from its checkpoint with the forward engine (one launch per step,
-// each into its own stash slot), then runs the chunk's adjoint steps.
+// each into its own stash slot), then runs the chunk's adjoint steps. With
+// fewer than 2C stash slots (a smaller memory budget) each chunk is
+// reversed by the binomial (revolve) schedule instead: a recursion that
+// advances from the newest stored state into a free slot, reverses the
+// right part with one slot fewer and then the left part, which is the
+// fewest forward steps any schedule with that many slots can take (Griewank
+// and Walther, ACM TOMS 26(1), 2000, Algorithm 799).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <mutex>
 #include <cstring>
 #include <vector>
@@ -513,16 +520,23 @@ __global__ void sum_parts_kernel(const double *part, int nblocks, int nt, double
 // ---------------------------------------------------------------------------
 struct Workspace {
   int ncp, C, nblocks, nt;
+  int slots;            // stash planes: 2C (two chunk buffers) or fewer (revolve)
+  bool revolve;         // chunks reversed by the binomial schedule
   size_t plane_bytes;
   size_t off_cp, off_stash, off_lam, off_hg, off_q, off_sd, off_part, total;
 };
 
-Workspace workspace_of(const gbs_desc *d, const Layout &L, int C) {
+// The stash holds two chunk buffers of C planes when slots >= 2C; with fewer
+// slots it holds `slots` snapshot planes plus two work planes of the
+// binomial schedule.
+Workspace workspace_of(const gbs_desc *d, const Layout &L, int C, int slots) {
   Workspace w{};
   const gbs_stencil_def_t *s = stencil_def(d->stencil);
   w.C = C;
   w.ncp = (d->timestep + C - 1) / C;
   if (w.ncp < 1) w.ncp = 1;
+  w.revolve = slots < 2 * C;
+  w.slots = w.revolve ? slots : 2 * C;
   w.plane_bytes = (size_t)L.plane * L.esize;
   const long long cells = (long long)L.dims[0] * L.dims[1] * L.dims[2];
   const bool grad = s->kind == 1;
@@ -530,7 +544,7 @@ Workspace workspace_of(const gbs_desc *d, const Layout &L, int C) {
   w.nt = grad ? 1 : std::min(s->nterms, kMaxCoefGrad);
   w.off_cp = 0;
   w.off_stash = w.off_cp + (size_t)w.ncp * w.plane_bytes;
-  w.off_lam = w.off_stash + 2 * (size_t)C * w.plane_bytes;  // two stash buffers
+  w.off_lam = w.off_stash + (size_t)(w.revolve ? w.slots + 2 : 2 * C) * w.plane_bytes;
   w.off_hg = w.off_lam + 2 * w.plane_bytes;
   w.off_q = w.off_hg + w.plane_bytes;
   w.off_sd = w.off_q + (grad ? w.plane_bytes : 0);
@@ -719,6 +733,53 @@ AdjKernels adj_kernels(int sid, int dtype) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// binomial (revolve) schedule
+// ---------------------------------------------------------------------------
+// beta(s, r) = (s + r)! / (s! r!): the most steps s snapshots reverse with
+// every step advanced at most r times (saturating)
+long long revolve_beta(int s, int r) {
+  long long v = 1;
+  for (int i = 1; i <= s; ++i) {
+    v = v * (r + i) / i;
+    if (v > (1LL << 40)) return 1LL << 40;
+  }
+  return v;
+}
+
+// Where to place the next snapshot when reversing l >= 2 steps from a stored
+// state with k >= 1 free snapshot slots (k + 1 stored states in all): r is
+// the least number of advances per step with beta(k+1, r) >= l. The split
+// m = l - beta(k, r-1), kept within [1, min(l-1, beta(k+1, r-1))], leaves
+// the right part (l - m steps, from the new snapshot, k - 1 slots left) as
+// long as r - 1 advances per step allow and the left part (m steps, k
+// slots) no longer than r - 1 advances allow; the total is then
+// r*l - beta(k+2, r-1) forward steps, the minimum (checked against an
+// exhaustive search over every split by the tests).
+int revolve_split(int l, int k) {
+  int r = 1;
+  while (revolve_beta(k + 1, r) < l) ++r;
+  long long m = l - revolve_beta(k, r - 1);
+  if (m < 1) m = 1;
+  const long long hi = std::min<long long>(l - 1, revolve_beta(k + 1, r - 1));
+  return (int)std::max(1LL, std::min(m, hi));
+}
+
+// forward steps the schedule takes to reverse l steps with s free slots, and
+// the most slots it holds at once
+void revolve_count(int l, int s, long long *steps, int *peak, int depth = 0) {
+  if (depth > *peak) *peak = depth;
+  if (l <= 1) return;
+  if (s == 0) {
+    *steps += (long long)l * (l - 1) / 2;
+    return;
+  }
+  const int m = revolve_split(l, s);
+  *steps += m;
+  revolve_count(l - m, s - 1, steps, peak, depth + 1);
+  revolve_count(m, s, steps, peak, depth);
+}
+
 gbs_status check_adjoint_args(const gbs_desc *d, int C, const void *ws) {
   gbs_status st = check_desc(d);
   if (st != GBS_OK) return st;
@@ -734,6 +795,55 @@ gbs_status check_adjoint_args(const gbs_desc *d, int C, const void *ws) {
     if (e_ != cudaSuccess) return cuda_fail(e_, what);   \
   } while (0)
 
+// Branch streams of the batched entry points, per device: work forked from
+// the caller's stream (an event), spread over the branches, joined back.
+constexpr int kBranches = 16;
+struct Branches {
+  cudaStream_t s[kBranches] = {};
+  cudaEvent_t fork = nullptr, join[kBranches] = {};
+};
+std::mutex g_branch_mu;  // held while a batched call enqueues (one set of events per device)
+Branches g_branches[64];
+
+gbs_status device_branches(Branches **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(GBS_ERR_NODEVICE, "device ordinal %d unsupported", dev);
+  Branches &b = g_branches[dev];
+  if (!b.fork) {
+    for (int k = 0; k < kBranches && e == cudaSuccess; ++k) {
+      e = cudaStreamCreateWithFlags(&b.s[k], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b.join[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint batch: branch streams");
+  }
+  *out = &b;
+  return GBS_OK;
+}
+
+// Runs run(i, branch_stream) for i < n on the branches (instance i on branch
+// i % kBranches), ordered after the work already on `stream`, and makes
+// `stream` wait for all of it.
+template <class F>
+gbs_status on_branches(int n, cudaStream_t stream, F run) {
+  std::lock_guard<std::mutex> lk(g_branch_mu);
+  Branches *b = nullptr;
+  gbs_status st = device_branches(&b);
+  if (st != GBS_OK) return st;
+  const int used = std::min(n, kBranches);
+  CK(cudaEventRecord(b->fork, stream), "adjoint batch: fork");
+  for (int k = 0; k < used; ++k) CK(cudaStreamWaitEvent(b->s[k], b->fork, 0), "adjoint batch: fork");
+  for (int i = 0; i < n && st == GBS_OK; ++i) st = run(i, b->s[i % kBranches]);
+  // join even after a failure, so that `stream` never runs ahead of work already enqueued
+  for (int k = 0; k < used; ++k) {
+    cudaEventRecord(b->join[k], b->s[k]);
+    cudaStreamWaitEvent(stream, b->join[k], 0);
+  }
+  return st;
+}
+
 }  // namespace
 }  // namespace gbs
 
@@ -742,11 +852,73 @@ using namespace gbs;
 extern "C" {
 
 gbs_status gbs_adjoint_workspace(const gbs_desc *d, int checkpoint_every, size_t *bytes) {
+  return gbs_adjoint_workspace_slots(d, checkpoint_every, 2 * std::max(1, checkpoint_every), bytes);
+}
+
+gbs_status gbs_adjoint_workspace_slots(const gbs_desc *d, int checkpoint_every, int slots, size_t *bytes) {
   gbs_status st = check_desc(d);
   if (st != GBS_OK) return st;
   if (checkpoint_every < 1 || !bytes) return fail(GBS_ERR_INVALID, "bad checkpoint interval or NULL bytes");
+  if (slots < 0) return fail(GBS_ERR_INVALID, "slots must be >= 0");
   const Layout L = make_layout(d);
-  *bytes = workspace_of(d, L, checkpoint_every).total;
+  *bytes = workspace_of(d, L, checkpoint_every, slots).total;
+  return GBS_OK;
+}
+
+gbs_status gbs_revolve_cost(int steps, int slots, long long *forward_steps, int *peak_slots) {
+  if (steps < 0 || slots < 0 || !forward_steps) return fail(GBS_ERR_INVALID, "bad revolve arguments");
+  long long n = 0;
+  int peak = 0;
+  revolve_count(steps, slots, &n, &peak);
+  *forward_steps = n;
+  if (peak_slots) *peak_slots = peak;
+  return GBS_OK;
+}
+
+gbs_status gbs_adjoint_plan_budget(const gbs_desc *d, size_t budget_bytes, int *checkpoint_every, int *slots,
+                                   size_t *bytes) {
+  gbs_status st = check_desc(d);
+  if (st != GBS_OK) return st;
+  if (!checkpoint_every || !slots) return fail(GBS_ERR_INVALID, "NULL output");
+  const Layout L = make_layout(d);
+  const int T = std::max(1, d->timestep);
+  // every checkpoint interval C, every slot count: the fewest recomputed
+  // forward steps whose workspace fits (ties: the smaller workspace)
+  long long best_cost = -1;
+  size_t best_bytes = 0;
+  int best_c = 0, best_s = 0;
+  for (int C = 1; C <= T; ++C) {
+    const int ncp = (T + C - 1) / C;
+    const Workspace w0 = workspace_of(d, L, C, 0);
+    if (w0.total > budget_bytes) continue;
+    // slots that still fit: revolve below 2C, the double stash at 2C
+    const long long room = (long long)((budget_bytes - w0.total) / w0.plane_bytes);
+    int s = (int)std::min<long long>(room, 2LL * C);
+    long long cost;
+    if (s >= 2 * C) {
+      cost = (long long)T - ncp;  // each chunk recomputed once (its states after the checkpoint)
+    } else {
+      cost = 0;
+      for (int j = 0; j < ncp; ++j) {
+        long long n = 0;
+        int peak = 0;
+        revolve_count(std::min(C, T - j * C), s, &n, &peak);
+        cost += n;
+      }
+    }
+    const size_t b = workspace_of(d, L, C, s).total;
+    if (b > budget_bytes) continue;
+    if (best_cost < 0 || cost < best_cost || (cost == best_cost && b < best_bytes)) {
+      best_cost = cost;
+      best_bytes = b;
+      best_c = C;
+      best_s = s;
+    }
+  }
+  if (best_cost < 0) return fail(GBS_ERR_NOMEM, "no checkpoint schedule fits %zu bytes", budget_bytes);
+  *checkpoint_every = best_c;
+  *slots = best_s;
+  if (bytes) *bytes = best_bytes;
   return GBS_OK;
 }
 
@@ -758,7 +930,7 @@ gbs_status gbs_adjoint_forward(const gbs_desc *d, void *dev_A, int checkpoint_ev
   int *err = nullptr;
   if ((st = error_word(&err)) != GBS_OK) return st;
   const Layout L = make_layout(d);
-  const Workspace w = workspace_of(d, L, checkpoint_every);
+  const Workspace w = workspace_of(d, L, checkpoint_every, 2 * checkpoint_every);
   char *ws = static_cast<char *>(workspace);
   char *A = static_cast<char *>(dev_A);
   cudaStream_t s = (cudaStream_t)stream;
@@ -780,8 +952,16 @@ gbs_status gbs_adjoint_forward(const gbs_desc *d, void *dev_A, int checkpoint_ev
 
 gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *dev_grad_u0, double *dev_coef_grad,
                                 int checkpoint_every, void *workspace, void *stream) {
+  return gbs_adjoint_backward_slots(d, dev_lamT, dev_grad_u0, dev_coef_grad, checkpoint_every,
+                                    2 * std::max(1, checkpoint_every), workspace, stream);
+}
+
+gbs_status gbs_adjoint_backward_slots(const gbs_desc *d, const void *dev_lamT, void *dev_grad_u0,
+                                      double *dev_coef_grad, int checkpoint_every, int slots, void *workspace,
+                                      void *stream) {
   gbs_status st = check_adjoint_args(d, checkpoint_every, workspace);
   if (st != GBS_OK) return st;
+  if (slots < 0) return fail(GBS_ERR_INVALID, "slots must be >= 0");
   if (!dev_lamT || !dev_grad_u0) return fail(GBS_ERR_INVALID, "NULL lam_T or grad_u0");
   const gbs_stencil_def_t *sd = stencil_def(d->stencil);
   const bool gradient = sd->kind == 1;
@@ -790,7 +970,7 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
   int *err = nullptr;
   if ((st = error_word(&err)) != GBS_OK) return st;
   const Layout L = make_layout(d);
-  const Workspace w = workspace_of(d, L, checkpoint_every);
+  const Workspace w = workspace_of(d, L, checkpoint_every, slots);
   const AdjGeom g = geom_of(L);
   char *ws = static_cast<char *>(workspace);
   cudaStream_t s = (cudaStream_t)stream;
@@ -840,6 +1020,64 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
     // no forward state enters: T transposed steps from lam_T
     for (int t = d->timestep - 1; t >= 0; --t)
       if ((st = step(nullptr)) != GBS_OK) return st;
+  } else if (w.revolve) {
+    // Each chunk reversed by the binomial schedule over `slots` snapshot
+    // planes and two work planes, all on `s`. The halo of every stash plane
+    // is the fixed boundary (copied once; launches never write it).
+    for (int k = 0; k < w.slots + 2; ++k)
+      CK(cudaMemcpyAsync(stash + (size_t)k * w.plane_bytes, ws + w.off_cp, w.plane_bytes, cudaMemcpyDeviceToDevice,
+                         s),
+         "adjoint: stash");
+    char *work0 = stash + (size_t)w.slots * w.plane_bytes;  // ping-pong partner of an advance
+    char *work1 = work0 + w.plane_bytes;                     // target of a recompute without slots
+    gbs_plan_info pi{};
+    {
+      gbs_desc dp = *d;
+      dp.timestep = std::max(1, w.C);
+      if ((st = gbs_plan(&dp, &pi)) != GBS_OK) return st;
+    }
+    const int bfwd = std::max(1, pi.bt);
+    // advance k >= 1 steps from plane src into plane dst (dst != work0)
+    auto advance = [&](const char *src, char *dst, int k) -> gbs_status {
+      const std::vector<int> blocks_k = split_steps(k, bfwd);
+      const int n = (int)blocks_k.size();
+      const char *from = src;
+      for (int j = 0; j < n; ++j) {
+        char *to = ((n - 1 - j) % 2 == 0) ? dst : work0;
+        gbs_status r = launch_block(d, L, coef.data(), div, eps, 0, blocks_k[j], from, to, s, err);
+        if (r != GBS_OK) return r;
+        from = to;
+      }
+      return GBS_OK;
+    };
+    // reverse steps [a, b) given u_a in plane ua, with `nfree` snapshot slots
+    // free from index `top` on
+    std::function<gbs_status(int, int, const char *, int)> reverse = [&](int a, int b, const char *ua,
+                                                                         int top) -> gbs_status {
+      const int l = b - a, nfree = w.slots - top;
+      if (l <= 0) return GBS_OK;
+      if (l == 1) return step(ua);
+      if (nfree == 0) {
+        for (int t = b - 1; t > a; --t) {
+          gbs_status r = advance(ua, work1, t - a);
+          if (r == GBS_OK) r = step(work1);
+          if (r != GBS_OK) return r;
+        }
+        return step(ua);
+      }
+      const int m = revolve_split(l, nfree);
+      char *snap = stash + (size_t)top * w.plane_bytes;
+      gbs_status r = advance(ua, snap, m);
+      if (r == GBS_OK) r = reverse(a + m, b, snap, top + 1);
+      if (r == GBS_OK) r = reverse(a, a + m, ua, top);
+      return r;
+    };
+    for (int j = w.ncp - 1; j >= 0 && st == GBS_OK; --j) {
+      const int t0 = j * w.C;
+      const int c = std::min(w.C, d->timestep - t0);
+      st = reverse(t0, t0 + c, ws + w.off_cp + (size_t)j * w.plane_bytes, 0);
+    }
+    if (st != GBS_OK) return st;
   } else {
     // Two stash buffers: while the adjoint steps of chunk j run on `s`, a
     // second stream recomputes the states of chunk j-1 into the other
@@ -922,6 +1160,35 @@ gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *d
   if (dev_coef_grad) sum_parts_kernel<<<w.nt, 256, 0, s>>>(part, w.nblocks, w.nt, dev_coef_grad);
   CK(cudaGetLastError(), "adjoint: combine");
   return GBS_OK;
+}
+
+gbs_status gbs_adjoint_forward_batch(const gbs_desc *descs, int n, void *const *dev_A, int checkpoint_every,
+                                     void *const *workspaces, void *stream) {
+  if (!descs || n < 1 || !dev_A || !workspaces) return fail(GBS_ERR_INVALID, "adjoint batch: no instances");
+  for (int i = 0; i < n; ++i) {
+    gbs_status st = check_adjoint_args(&descs[i], checkpoint_every, workspaces[i]);
+    if (st != GBS_OK) return st;
+    if (!dev_A[i]) return fail(GBS_ERR_INVALID, "adjoint batch: instance %d has no grid", i);
+  }
+  return on_branches(n, (cudaStream_t)stream, [&](int i, cudaStream_t bs) {
+    return gbs_adjoint_forward(&descs[i], dev_A[i], checkpoint_every, workspaces[i], bs);
+  });
+}
+
+gbs_status gbs_adjoint_backward_batch(const gbs_desc *descs, int n, const void *const *dev_lamT,
+                                      void *const *dev_grad_u0, double *const *dev_coef_grad, int checkpoint_every,
+                                      void *const *workspaces, void *stream) {
+  if (!descs || n < 1 || !dev_lamT || !dev_grad_u0 || !workspaces)
+    return fail(GBS_ERR_INVALID, "adjoint batch: no instances");
+  for (int i = 0; i < n; ++i) {
+    gbs_status st = check_adjoint_args(&descs[i], checkpoint_every, workspaces[i]);
+    if (st != GBS_OK) return st;
+    if (!dev_lamT[i] || !dev_grad_u0[i]) return fail(GBS_ERR_INVALID, "adjoint batch: instance %d lacks a plane", i);
+  }
+  return on_branches(n, (cudaStream_t)stream, [&](int i, cudaStream_t bs) {
+    return gbs_adjoint_backward(&descs[i], dev_lamT[i], dev_grad_u0[i], dev_coef_grad ? dev_coef_grad[i] : nullptr,
+                                checkpoint_every, workspaces[i], bs);
+  });
 }
 
 }  // extern "C"

@@ -279,7 +279,10 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
   for (int g = 0; g < ngrids; ++g) {
     const gbs_batch_grid &bg = grids[g];
     const gbs_stencil_def_t *s = stencil_def(bg.stencil);
-    if (!s || s->dim != 2) return fail(GBS_ERR_INVALID, "batch grid %d: not a 2-D stencil", g);
+    if (!s) return fail(GBS_ERR_INVALID, "batch grid %d: unknown stencil %d", g, bg.stencil);
+    if (s->dim != 2)
+      return fail(GBS_ERR_UNSUPPORTED, "batch grid %d: the work-item schedules take 2-D grids (use GBS_BATCH_STREAMS)",
+                  g);
     if (bg.n[0] < 1 || bg.n[1] < 1 || bg.timestep < 0 || !bg.dev_A)
       return fail(GBS_ERR_INVALID, "batch grid %d: bad extent, timestep or buffer", g);
     if (reinterpret_cast<uintptr_t>(bg.dev_A) % 128 != 0)
@@ -476,7 +479,8 @@ gbs_status run(const gbs_batch_grid *grids, int ngrids, cudaStream_t stream) {
   for (int g = 0; g < ngrids; ++g) {
     const gbs_batch_grid &bg = grids[g];
     const gbs_stencil_def_t *s = stencil_def(bg.stencil);
-    if (!s || s->dim != 2) return fail(GBS_ERR_INVALID, "batch grid %d: not a 2-D stencil", g);
+    if (!s) return fail(GBS_ERR_INVALID, "batch grid %d: unknown stencil %d", g, bg.stencil);
+    if (s->dim != 2) return fail(GBS_ERR_UNSUPPORTED, "batch grid %d: the run without allocation takes 2-D grids", g);
     if (bg.n[0] < 1 || bg.n[1] < 1 || bg.timestep < 0 || !bg.dev_A)
       return fail(GBS_ERR_INVALID, "batch grid %d: bad extent, timestep or buffer", g);
     if (reinterpret_cast<uintptr_t>(bg.dev_A) % 128 != 0)
@@ -628,7 +632,7 @@ int branches() {
   return n >= 1 && n <= kMaxStreams ? n : kStreams;
 }
 
-gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, gbs_batch **out) {
+gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, gbs_batch **out) {
   if (!grids || ngrids <= 0) return fail(GBS_ERR_INVALID, "batch: no grids");
   const int nbr = branches();
   std::vector<gbs_desc> ds(ngrids);
@@ -638,18 +642,18 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
   for (int g = 0; g < ngrids; ++g) {
     const gbs_batch_grid &bg = grids[g];
     const gbs_stencil_def_t *s = stencil_def(bg.stencil);
-    if (!s || s->dim != 2) return fail(GBS_ERR_INVALID, "batch grid %d: not a 2-D stencil", g);
-    if (bg.n[0] < 1 || bg.n[1] < 1 || bg.timestep < 0 || !bg.dev_A)
+    if (!s) return fail(GBS_ERR_INVALID, "batch grid %d: unknown stencil %d", g, bg.stencil);
+    if (bg.n[0] < 1 || bg.n[1] < 1 || (s->dim == 3 && bg.n[2] < 1) || bg.timestep < 0 || !bg.dev_A)
       return fail(GBS_ERR_INVALID, "batch grid %d: bad extent, timestep or buffer", g);
     if (reinterpret_cast<uintptr_t>(bg.dev_A) % 128 != 0)
       return fail(GBS_ERR_INVALID, "batch grid %d: buffer not 128-byte aligned", g);
     gbs_desc &d = ds[g];
     d = gbs_desc{};
     d.stencil = bg.stencil;
-    d.dtype = GBS_F32;
+    d.dtype = dtype;
     d.n[0] = bg.n[0];
     d.n[1] = bg.n[1];
-    d.n[2] = 1;
+    d.n[2] = s->dim == 3 ? bg.n[2] : 1;
     d.timestep = bg.timestep;
     d.fp_mode = fp_mode;
     d.coef = bg.coef;
@@ -663,16 +667,17 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int fp_mode, g
     // measured faster on GB300: 254 vs 220 GCells/s at 16 branches)
     d.bt = pi.bt;
     const char *share_env = std::getenv("GBS_BATCH_SHARE");
-    if (d.sl == 0 && share_env && share_env[0] == '1') {
+    if (s->dim == 2 && d.sl == 0 && share_env && share_env[0] == '1') {
       const Layout L = make_layout(&d);
       const int fma = fp_mode == GBS_FP_FMA ? 1 : 0;
-      const long long share = std::max<long long>(1, resident_warps_2d(d.stencil, GBS_F32, fma, pi.bt) / nbr);
+      const long long share = std::max<long long>(1, resident_warps_2d(d.stencil, dtype, fma, pi.bt) / nbr);
       d.sl = geometry2d(L, pi.bt, 0, share).sl;
       if ((st = gbs_plan(&d, &pi)) != GBS_OK) return st;
     }
     launches += pi.launches;
-    cells += (long long)bg.n[0] * bg.n[1] * bg.timestep;
-    work[g] = (double)bg.n[0] * bg.n[1] * bg.timestep;
+    const long long area = (long long)d.n[0] * d.n[1] * (s->dim == 3 ? d.n[2] : 1);
+    cells += area * bg.timestep;
+    work[g] = (double)area * bg.timestep;
   }
   int *err = nullptr;
   gbs_status st = error_word(&err);
@@ -744,12 +749,14 @@ gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, in
                           gbs_batch **out) {
   if (mode != GBS_BATCH_PERSISTENT && mode != GBS_BATCH_LAYERED && mode != GBS_BATCH_STREAMS)
     return fail(GBS_ERR_INVALID, "bad batch mode");
-  if (dtype != GBS_F32) return fail(GBS_ERR_UNSUPPORTED, "batched launch supports GBS_F32 grids");
+  if (dtype != GBS_F32 && dtype != GBS_F64) return fail(GBS_ERR_INVALID, "bad dtype");
+  if (dtype != GBS_F32 && mode != GBS_BATCH_STREAMS)
+    return fail(GBS_ERR_UNSUPPORTED, "the work-item schedules take GBS_F32 grids (use GBS_BATCH_STREAMS)");
   if (fp_mode != GBS_FP_EXACT && fp_mode != GBS_FP_FMA) return fail(GBS_ERR_INVALID, "bad fp_mode");
   if (!out) return fail(GBS_ERR_INVALID, "out is NULL");
   gbs_batch *h = nullptr;
   gbs_status st;
-  if (mode == GBS_BATCH_STREAMS) st = build_streams(grids, ngrids, fp_mode, &h);
+  if (mode == GBS_BATCH_STREAMS) st = build_streams(grids, ngrids, dtype, fp_mode, &h);
   else st = fp_mode == GBS_FP_FMA ? gbs_batch_build_1(grids, ngrids, mode, &h)
                                   : gbs_batch_build_0(grids, ngrids, mode, &h);
   *out = h;

@@ -97,6 +97,11 @@ gbs_status check_desc(const gbs_desc *d) {
   if (d->timestep < 0) return fail(GBS_ERR_INVALID, "timestep must be >= 0 (got %d)", d->timestep);
   if (d->bt < 0 || d->sl < 0 || d->bs1 < 0 || d->bs2 < 0)
     return fail(GBS_ERR_INVALID, "bt/bs1/bs2/sl must be >= 0");
+  const int V = d->dtype == GBS_F64 ? 2 : 4;
+  if (d->bs2 != 0 && d->bs2 != 32 * V)
+    return fail(GBS_ERR_UNSUPPORTED, "bs2 (tile columns) must be 0 or %d for this element type", 32 * V);
+  if (s->dim == 2 && d->bs1 != 0 && d->bs1 != kWarpsPerCta2D)
+    return fail(GBS_ERR_UNSUPPORTED, "bs1 (warps per CTA) of a 2-D grid must be 0 or %d", kWarpsPerCta2D);
   return GBS_OK;
 }
 
@@ -256,29 +261,51 @@ Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident) {
   return g;
 }
 
-long long resident_ctas_3d(int sid, int dtype, int fma, int b) {
+long long resident_ctas_3d(int sid, int dtype, int fma, int b, int v) {
   static std::mutex mu;
-  static int cache[kNumStencils][2][2][kMaxB + 1];
+  static int cache[kNumStencils][2][2][kMaxB + 1][kVar3];
   std::lock_guard<std::mutex> lk(mu);
-  int &c = cache[sid][dtype][fma][b];
+  if (b < 1 || b > kMaxB || v < 0 || v >= kVar3) return sm_count();
+  int &c = cache[sid][dtype][fma][b][v];
   if (c == 0) {
     const Picks &pk = picks(sid, dtype, fma);
-    int n = (b <= kMaxB && pk.o3[b]) ? pk.o3[b]() : 0;
+    int n = pk.o3[b][v] ? pk.o3[b][v]() : 0;
     c = n > 0 ? n : 1;
   }
   return (long long)c * sm_count();
 }
 
-Tile3DShape tile_shape_3d(int sid, int dtype, int fma, int b) {
+Tile3DShape tile_shape_3d(int sid, int dtype, int fma, int b, int v) {
   const Picks &pk = picks(sid, dtype, fma);
   Tile3DShape t{};
-  if (b >= 1 && b <= kMaxB && pk.tj3[b] > 0) {
-    t.tj = pk.tj3[b];
-    t.jout = pk.jout3[b];
-    t.wk = pk.wk3[b];
+  if (b >= 1 && b <= kMaxB && v >= 0 && v < kVar3 && pk.tj3[b][v] > 0) {
+    t.tj = pk.tj3[b][v];
+    t.jout = pk.jout3[b][v];
+    t.wk = pk.wk3[b][v];
     t.tile = pk.tile3[b];
   }
   return t;
+}
+
+int variant_3d(const gbs_desc *d, int b) {
+  const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
+  const Picks &pk = picks(d->stencil, d->dtype, fma);
+  if (b < 1 || b > kMaxB) return -1;
+  int want = d->bs1;
+  if (want <= 0) {
+    int tb = 0, ts = 0, tr = 0;
+    if (tuned_lookup(d, &tb, &ts, &tr) && tb == b) want = tr;
+  }
+  if (want > 0) {
+    for (int v = 0; v < kVar3; ++v)
+      if (pk.tj3[b][v] == want) return v;
+    if (d->bs1 > 0) {
+      fail(GBS_ERR_UNSUPPORTED, "no 3-D tile of %d rows at degree %d (built: %d, %d)", d->bs1, b, pk.tj3[b][0],
+           pk.tj3[b][1]);
+      return -1;
+    }
+  }
+  return 0;
 }
 
 // Tiles of the launcher's shape (rows x one 32*V-column window); the number
@@ -479,8 +506,10 @@ gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, 
       cudaError_t e = pk.l2[b](a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");
     } else {
-      Geometry3D g = geometry3d(L, b, tile_shape_3d(d->stencil, d->dtype, fma, b), sl,
-                                 resident_ctas_3d(d->stencil, d->dtype, fma, b));
+      const int v = variant_3d(d, b);
+      if (v < 0) return GBS_ERR_UNSUPPORTED;
+      Geometry3D g = geometry3d(L, b, tile_shape_3d(d->stencil, d->dtype, fma, b, v), sl,
+                                 resident_ctas_3d(d->stencil, d->dtype, fma, b, v));
       gbs_status st = validate3d(L, g);
       if (st != GBS_OK) return st;
       Launch3D a{};
@@ -502,8 +531,8 @@ gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, 
       a.coef = coef;
       a.div = div;
       a.div_proven = d->dtype == GBS_F32 && div_proven_exact(div);
-      if (!pk.l3[b]) return fail(GBS_ERR_UNSUPPORTED, "no 3-D kernel for b=%d", b);
-      cudaError_t e = pk.l3[b](a, stream);
+      if (!pk.l3[b][v]) return fail(GBS_ERR_UNSUPPORTED, "no 3-D kernel for b=%d", b);
+      cudaError_t e = pk.l3[b][v](a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "3-D stencil launch");
     }
   }
@@ -577,15 +606,18 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
     Geometry2D g = geometry2d(L, bt, sl, resident_warps_2d(d->stencil, d->dtype, fma, bt));
     st = validate2d(L, g);
     if (st != GBS_OK) return st;
-    out->bs1 = 4;
+    out->bs1 = kWarpsPerCta2D;
+    out->bs2 = 32 * L.V;
     out->sl = g.sl;
     out->ctas = (g.nstrips * g.nblocks + 3) / 4;
     out->valid_w = g.wout;
     const double cols = 32.0 * L.V, rows = g.sl + 2.0 * bt * L.rad;
     out->redundancy = (cols * rows) / ((double)g.wout * g.sl);
   } else {
-    Geometry3D g = geometry3d(L, bt, tile_shape_3d(d->stencil, d->dtype, fma, bt), sl,
-                                 resident_ctas_3d(d->stencil, d->dtype, fma, bt));
+    const int v = variant_3d(d, bt);
+    if (v < 0) return GBS_ERR_UNSUPPORTED;
+    Geometry3D g = geometry3d(L, bt, tile_shape_3d(d->stencil, d->dtype, fma, bt, v), sl,
+                                 resident_ctas_3d(d->stencil, d->dtype, fma, bt, v));
     st = validate3d(L, g);
     if (st != GBS_OK) return st;
     out->bs1 = g.tj;

@@ -36,10 +36,14 @@ struct Geometry3D {
 struct Tile3DShape {
   int tj, jout, wk, tile;
 };
-Tile3DShape tile_shape_3d(int sid, int dtype, int fma, int b);
+Tile3DShape tile_shape_3d(int sid, int dtype, int fma, int b, int variant);
+// block-shape variant of the 3-D launcher of degree b for d: the one whose
+// tile rows equal d->bs1, else the tuning table's, else variant 0; -1 (and
+// an error recorded) when d->bs1 names no built shape
+int variant_3d(const gbs_desc *d, int b);
 Geometry3D geometry3d(const Layout &L, int b, const Tile3DShape &ts, int sl_req, long long resident_ctas);
 gbs_status validate3d(const Layout &L, const Geometry3D &g);
-long long resident_ctas_3d(int sid, int dtype, int fma, int b);
+long long resident_ctas_3d(int sid, int dtype, int fma, int b, int variant);
 
 gbs_status fail(gbs_status st, const char *fmt, ...);
 gbs_status cuda_fail(cudaError_t e, const char *what);
@@ -57,7 +61,7 @@ gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, 
                         int b, const void *src, void *dst, cudaStream_t stream, int *err);
 int max_bt(int sid, int dtype, int fma);
 // the tuning table's (bt, sl) for d's stencil, dtype, mode and size class
-bool tuned_lookup(const gbs_desc *d, int *bt, int *sl);
+bool tuned_lookup(const gbs_desc *d, int *bt, int *sl, int *bs1 = nullptr);
 bool div_proven_exact(double d);
 
 }  // namespace gbs

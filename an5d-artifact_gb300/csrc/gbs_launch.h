@@ -41,16 +41,22 @@ using Occupancy3DFn = int (*)();
 // Launchers of one (stencil, element type, fp mode), indexed by the fused
 // degree b (nullptr where none is built).
 constexpr int kMaxB = 16;
+// warps per CTA of the 2-D kernels (each warp streams its own work items)
+constexpr int kWarpsPerCta2D = 4;
+// 3-D block shapes per degree: variant v of the tile kernel has kTileWarps[v]
+// warps (tile rows = warps x rows per warp)
+constexpr int kVar3 = 2;
+constexpr int kTileWarps[kVar3] = {16, 8};
 struct Picks {
   int maxb;
   Launch2DFn l2[kMaxB + 1];
   Occupancy2DFn o2[kMaxB + 1];
-  Launch3DFn l3[kMaxB + 1];
-  Occupancy3DFn o3[kMaxB + 1];
-  int tj3[kMaxB + 1];    // tile rows of the 3-D launcher
-  int jout3[kMaxB + 1];  // valid (output) rows of its tile
-  int wk3[kMaxB + 1];    // valid (output) columns of its tile
-  int tile3[kMaxB + 1];  // 1: the tensor-map tile kernel (no column window checks needed)
+  Launch3DFn l3[kMaxB + 1][kVar3];
+  Occupancy3DFn o3[kMaxB + 1][kVar3];
+  int tj3[kMaxB + 1][kVar3];    // tile rows of the 3-D launcher (0: variant not built)
+  int jout3[kMaxB + 1][kVar3];  // valid (output) rows of its tile
+  int wk3[kMaxB + 1][kVar3];    // valid (output) columns of its tile
+  int tile3[kMaxB + 1];         // 1: the tensor-map tile kernel (no column window checks needed)
 };
 
 // Encodes the tensor map of one time plane of a 3-D grid for the tile kernel:

@@ -63,17 +63,28 @@ constexpr int max_class() {
   return b;
 }
 
+// block-shape variant V of the 3-D launcher of degree B, when its tile keeps
+// outputs and fits in shared memory
+template <int B, int V> void add_variant3(Picks &p) {
+  constexpr int NW = kTileWarps[V];
+  if constexpr (tile_jout3d<S, T, B, kFma, NW>() > 0 && tile_wk3d<S, T, B, kFma, NW>() > 0 &&
+                smem_bytes3d<S, T, B, kFma, NW>() <= 227u * 1024u) {
+    p.l3[B][V] = &launch3d<S, T, B, kFma, NW>;
+    p.o3[B][V] = &occupancy3d<S, T, B, kFma, NW>;
+    p.tj3[B][V] = tile_rows3d<S, T, B, kFma, NW>();
+    p.jout3[B][V] = tile_jout3d<S, T, B, kFma, NW>();
+    p.wk3[B][V] = tile_wk3d<S, T, B, kFma, NW>();
+  }
+}
+
 template <int B> void add(Picks &p) {
   if constexpr (B <= max_class()) {
     if constexpr (S::kDim == 2) {
       p.l2[B] = &launch2d<S, T, B, kFma>;
       p.o2[B] = &occupancy2d<S, T, B, kFma>;
     } else {
-      p.l3[B] = &launch3d<S, T, B, kFma>;
-      p.o3[B] = &occupancy3d<S, T, B, kFma>;
-      p.tj3[B] = tile_rows3d<S, T, B, kFma>();
-      p.jout3[B] = tile_jout3d<S, T, B, kFma>();
-      p.wk3[B] = tile_wk3d<S, T, B, kFma>();
+      add_variant3<B, 0>(p);
+      if constexpr (use_tile3d<S, kFma>()) add_variant3<B, 1>(p);
       p.tile3[B] = use_tile3d<S, kFma>() ? 1 : 0;
     }
     p.maxb = B;

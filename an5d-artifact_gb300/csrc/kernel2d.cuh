@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(WPC * 32, gbs_min_ctas(WPC * 32))
   warp_item2d<ST, T, B, FMA, NSTAGE>(p, (int)(gw % p.nstrips), (int)(gw / p.nstrips), ring, bars, load_base);
 }
 
-constexpr int kWpc2D = 4, kStages2D = 16;
+constexpr int kWpc2D = kWarpsPerCta2D, kStages2D = 16;
 
 template <class ST, typename T, int B, bool FMA>
 int occupancy2d() {

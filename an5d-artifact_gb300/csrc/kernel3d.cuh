@@ -405,279 +405,6 @@ __global__ void __launch_bounds__(TJ * 32, gbs_min_ctas(TJ * 32))
   }
 }
 
-// ---------------------------------------------------------------------------
-// FMA-mode variant: H rows per warp. Each warp owns H consecutive tile rows
-// (TJ = NW*H), so per-step overheads (the stage wait, address arithmetic,
-// the store) are shared by H*V cells and every smem row a thread loads feeds
-// up to 2r+1 of its own output rows. The step loop is unrolled 2r+1 times
-// where the code stays small, so the partial sums rotate by renaming.
-// Intermediate levels (b > 1) fill their halo cells from a copy of the
-// fixed halo loaded from HBM one step ahead; with b == 1 no halo cell is
-// ever consumed, so none is fetched.
-// ---------------------------------------------------------------------------
-template <class ST, typename T, int B, int NW, int H>
-struct Rows3 {
-  static constexpr int R = ST::kRad;
-  static constexpr int W = 2 * R + 1;
-  static constexpr int V = 16 / sizeof(T);
-  static constexpr int ROW = 32 * V;
-  static constexpr int TJ = NW * H;
-  static constexpr int NS = 4;
-  static constexpr int DEP = 2;
-  static constexpr int PLANE = (TJ + 2 * R) * ROW;
-  static constexpr size_t bytes() {
-    return (size_t)PLANE * sizeof(T) * (NS + (size_t)(B - 1) * DEP) + NS * sizeof(uint64_t);
-  }
-  static constexpr bool UNR = W * ST::kTerms * H * V <= 4000;
-  static constexpr int NPH = UNR ? W : 1;
-};
-
-template <class ST, typename T, int B, int NW, int H>
-__global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
-    stencil3d_rows_kernel(const __grid_constant__ Params3D<T, ST::kTerms> p) {
-  using G = Rows3<ST, T, B, NW, H>;
-  constexpr int V = G::V, R = G::R, W = G::W, ROW = G::ROW, TJ = G::TJ;
-  constexpr int NS = G::NS, DEP = G::DEP, PLANE = G::PLANE, NPH = G::NPH;
-  constexpr bool UNR = G::UNR;
-  constexpr unsigned ROW_BYTES = ROW * sizeof(T);
-  using A = Arith<T>;
-  using OR = Order3<ST, true>;
-
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  T *ring0 = reinterpret_cast<T *>(smem_raw);
-  T *rings = ring0 + (size_t)NS * PLANE;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(rings + (size_t)(B - 1) * DEP * PLANE);
-
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
-  int bid = blockIdx.x;
-  const int tk = bid % p.ntk;
-  bid /= p.ntk;
-  const int tj = bid % p.ntj;
-  const int blk = bid / p.ntj;
-
-  const int cs = R + tk * p.wk;
-  const int ce = min(cs + p.wk, p.d2 - R);
-  const int ws = ((max(0, cs - B * R) + p.shift) / V) * V;
-  const int col0 = ws - p.shift + lane * V;
-  const bool kedge = (ws - p.shift < R) || (ws - p.shift + ROW > p.d2 - R);
-  const bool store_all = (col0 >= cs && col0 + V <= ce);
-  const int js = R + tj * p.jout;
-  const int je = min(js + p.jout, p.d1 - R);
-  const int j0 = js - B * R + w * H;  // global row of this warp's first row
-  const int i0 = R + blk * p.sl;
-  const int i1 = min(i0 + p.sl, p.d0 - R);
-  const int pstart = max(0, i0 - B * R);
-  const int pend = min(p.d0, i1 + B * R);
-  const int slast = i1 - 1 + (B - 1) + B * R;
-  const long long plane_stride = (long long)p.d1 * p.pitch;
-  bool warp_jhalo = false;
-#pragma unroll
-  for (int h = 0; h < H; ++h) warp_jhalo |= (j0 + h < R || j0 + h >= p.d1 - R);
-
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], TJ);
-    fence_mbar_init();
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-
-  // lanes 0..H-1 of every warp copy one row each of `plane`
-  auto issue = [&](int plane) {
-    if (lane < H) {
-      const int n = plane - pstart;
-      const int st = n % NS;
-      const int jr = j0 + lane;
-      if (jr >= 0 && jr < p.d1) {
-        mbar_arrive_expect_tx(&bars[st], ROW_BYTES);
-        bulk_g2s(ring0 + (size_t)st * PLANE + (size_t)(w * H + lane + R) * ROW,
-                 p.src + plane * plane_stride + (long long)jr * p.pitch + ws, ROW_BYTES, &bars[st]);
-      } else {
-        mbar_arrive(&bars[st]);
-      }
-    }
-  };
-  for (int pl = pstart; pl < pend && pl < pstart + NS; ++pl) issue(pl);
-
-  T acc[B][W][H][V];
-  static_for<B>([&](auto LI) {
-    static_for<W>([&](auto AI) {
-      static_for<H>([&](auto HI) {
-        static_for<V>([&](auto EI) {
-          acc[decltype(LI)::value][decltype(AI)::value][decltype(HI)::value][decltype(EI)::value] = T(0);
-        });
-      });
-    });
-  });
-  // fixed-halo values of the next step's output plane, per intermediate level
-  constexpr int BC = B > 1 ? B - 1 : 1;
-  T cr[BC][H][V];
-  bool crv[BC];
-#pragma unroll
-  for (int l = 0; l < BC; ++l) crv[l] = false;
-
-  bool ok = true;
-  int waited = pstart;
-  auto wait_plane = [&](int pl) -> bool {
-    bool got = true;
-    if (pl < pend) {
-      const int n = pl - pstart;
-      got = mbar_wait(&bars[n % NS], (unsigned)(n / NS) & 1u, nullptr, 0);
-    }
-    if (!__syncthreads_and(got)) {
-      if (threadIdx.x == 0) atomicOr(p.err, ERR_WAIT_TIMEOUT);
-      return false;
-    }
-    if (pl < pend) waited = pl + 1;
-    return true;
-  };
-  // issues the halo copies level l needs at step s (output plane q)
-  auto fetch_carry = [&](auto LI, int s) {
-    constexpr int l = decltype(LI)::value;
-    const int q = s - l * (R + 1) - R;
-    const bool need = (q >= 0 && q < p.d0) && (q < R || q >= p.d0 - R || warp_jhalo || kedge);
-    crv[l] = need;
-    if (need) {
-      static_for<H>([&](auto HI) {
-        constexpr int h = decltype(HI)::value;
-        const int jr = j0 + h;
-        if (jr >= 0 && jr < p.d1)
-          ld_vec_global<T, V>(cr[l][h], p.src + q * plane_stride + (long long)jr * p.pitch + ws + lane * V);
-      });
-    }
-  };
-
-  auto step = [&](auto PHI, int s) {
-    constexpr int ph = decltype(PHI)::value;
-    if (s > pstart && lane < H) {
-      const int pf = s - 1 + NS;
-      if (pf >= pstart + NS && pf < pend) issue(pf);
-    }
-    static_for<B>([&](auto LI) {
-      constexpr int l = decltype(LI)::value;
-      const int m = s - l * (R + 1);
-      const int q = m - R;
-      const T *in_m;
-      if constexpr (l == 0) in_m = ring0 + (size_t)((m - pstart) % NS) * PLANE;
-      else in_m = rings + (size_t)(l - 1) * DEP * PLANE + (size_t)(((s - 1) % DEP + DEP) % DEP) * PLANE;
-      // rows rho = -R .. H+R-1 relative to the warp's first row
-      static_for<H + 2 * R>([&](auto RI) {
-        constexpr int rho = decltype(RI)::value - R;
-        constexpr bool used = [] {
-          for (int t = 0; t < ST::kTerms; ++t) {
-            const int hh = rho - ST::kOff[t][1];
-            if (hh >= 0 && hh < H) return true;
-          }
-          return false;
-        }();
-        if constexpr (used) {
-          T row[V];
-          ld_vec<T, V>(row, in_m + (size_t)(w * H + R + rho) * ROW + lane * V);
-          T ext[V + 2 * R];
-          static_for<V + 2 * R>([&](auto XI) {
-            constexpr int xx = decltype(XI)::value - R;
-            constexpr bool nx = [] {
-              for (int t = 0; t < ST::kTerms; ++t) {
-                const int hh = rho - ST::kOff[t][1];
-                const int e = xx - ST::kOff[t][2];
-                if (hh >= 0 && hh < H && e >= 0 && e < V) return true;
-              }
-              return false;
-            }();
-            if constexpr (nx) ext[R + xx] = row_elem<V, xx>(row);
-          });
-          static_for<ST::kTerms>([&](auto UI) {
-            constexpr int u = decltype(UI)::value;
-            constexpr int t = OR::idx.v[u];
-            constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
-            constexpr int h = rho - dj;
-            if constexpr (h >= 0 && h < H) {
-              constexpr int slot = wslot<UNR, W>(ph, R - di);
-              static_for<V>([&](auto EI) {
-                constexpr int e = decltype(EI)::value;
-                const T a = ext[R + e + dk];
-                if constexpr (u == OR::init_pos()) acc[l][slot][h][e] = A::mul(p.coef[t], a);
-                else acc[l][slot][h][e] = A::fma(p.coef[t], a, acc[l][slot][h][e]);
-              });
-            }
-          });
-        }
-      });
-      constexpr int oslot = wslot<UNR, W>(ph, 0);
-      if constexpr (l + 1 < B) {
-        // intermediate level: fill halo cells, publish the plane
-        T *out = rings + (size_t)l * DEP * PLANE + (size_t)(s % DEP) * PLANE;
-        static_for<H>([&](auto HI) {
-          constexpr int h = decltype(HI)::value;
-          T y[V];
-          static_for<V>([&](auto EI) { y[decltype(EI)::value] = acc[l][oslot][h][decltype(EI)::value]; });
-          if (crv[l]) {
-            const int jr = j0 + h;
-            const bool rowhalo = (q < R || q >= p.d0 - R || jr < R || jr >= p.d1 - R);
-            static_for<V>([&](auto EI) {
-              constexpr int e = decltype(EI)::value;
-              if (rowhalo || col0 + e < R || col0 + e >= p.d2 - R) y[e] = cr[l][h][e];
-            });
-          }
-          st_vec<T, V>(out + (size_t)(w * H + R + h) * ROW + lane * V, y);
-        });
-        fetch_carry(LI, s + 1);
-      } else {
-        if (q >= i0 && q < i1) {
-          static_for<H>([&](auto HI) {
-            constexpr int h = decltype(HI)::value;
-            const int jr = j0 + h;
-            if (jr >= js && jr < je) {
-              T *d = p.dst + q * plane_stride + (long long)jr * p.pitch + ws + lane * V;
-              if (store_all) {
-                st_vec<T, V>(d, acc[l][oslot][h]);
-              } else {
-                static_for<V>([&](auto EI) {
-                  constexpr int e = decltype(EI)::value;
-                  if (col0 + e >= cs && col0 + e < ce) d[e] = acc[l][oslot][h][e];
-                });
-              }
-            }
-          });
-        }
-      }
-      if constexpr (!UNR) {
-        static_for<2 * R>([&](auto AI) {
-          constexpr int a = decltype(AI)::value;
-          static_for<H>([&](auto HI) {
-            static_for<V>([&](auto EI) {
-              acc[l][a][decltype(HI)::value][decltype(EI)::value] = acc[l][a + 1][decltype(HI)::value][decltype(EI)::value];
-            });
-          });
-        });
-      }
-    });
-    ok = wait_plane(s + 1);
-  };
-
-  if constexpr (B > 1) {
-    static_for<B - 1>([&](auto LI) { fetch_carry(LI, pstart); });
-  }
-  ok = wait_plane(pstart);
-#pragma unroll 1
-  for (int sb = pstart; ok && sb <= slast; sb += NPH) {
-    static_for<NPH>([&](auto PHI) {
-      const int s = sb + decltype(PHI)::value;
-      if (!ok || s > slast) return;
-      step(PHI, s);
-    });
-  }
-
-  if (!ok && lane < H) {
-    const int last = min(pend, waited + NS);
-    for (int pl = waited; pl < last; ++pl) {
-      const int n = pl - pstart;
-      if (!mbar_wait(&bars[n % NS], (unsigned)(n / NS) & 1u, p.err, ERR_DRAIN_TIMEOUT)) break;
-    }
-  }
-}
-
 }  // namespace gbs
 
 #include "kernel3d_tile.cuh"
@@ -709,53 +436,53 @@ template <class ST, bool FMA>
 constexpr bool use_tile3d() { return FMA && ST::kTerms <= 125; }
 
 // level-0 stages of the tile kernel: four, or three where four do not fit
-template <class ST, typename T, int B>
+template <class ST, typename T, int B, int NW>
 constexpr int tile_stages3d() {
-  return Tile3<ST, T, B, kNw3D, rows_per_warp<ST, T, B>(), 4>::bytes() <= 227u * 1024u ? 4 : 3;
+  return Tile3<ST, T, B, NW, rows_per_warp<ST, T, B>(), 4>::bytes() <= 227u * 1024u ? 4 : 3;
 }
-template <class ST, typename T, int B>
-using TileOf = Tile3<ST, T, B, kNw3D, rows_per_warp<ST, T, B>(), tile_stages3d<ST, T, B>()>;
+template <class ST, typename T, int B, int NW = kNw3D>
+using TileOf = Tile3<ST, T, B, NW, rows_per_warp<ST, T, B>(), tile_stages3d<ST, T, B, NW>()>;
 
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 constexpr int tile_rows3d() {
-  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B>::TJ : kTj3D;
+  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B, NW>::TJ : kTj3D;
 }
 
 // valid rows and columns per tile of the launcher for (ST, T, B, FMA)
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 constexpr int tile_jout3d() {
-  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B>::JOUT : kTj3D - 2 * B * ST::kRad;
+  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B, NW>::JOUT : kTj3D - 2 * B * ST::kRad;
 }
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 constexpr int tile_wk3d() {
   constexpr int V = 16 / sizeof(T);
-  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B>::WK : (32 * V - 2 * B * ST::kRad - (V - 1)) / V * V;
+  return use_tile3d<ST, FMA>() ? TileOf<ST, T, B, NW>::WK : (32 * V - 2 * B * ST::kRad - (V - 1)) / V * V;
 }
 
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 constexpr size_t smem_bytes3d() {
-  if constexpr (use_tile3d<ST, FMA>()) return TileOf<ST, T, B>::bytes();
+  if constexpr (use_tile3d<ST, FMA>()) return TileOf<ST, T, B, NW>::bytes();
   else return Smem3<ST, T, FMA>::bytes(kTj3D, B);
 }
 
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 auto kernel3d_ptr() {
   if constexpr (use_tile3d<ST, FMA>()) {
-    using G = TileOf<ST, T, B>;
-    return stencil3d_tile_kernel<ST, T, B, kNw3D, rows_per_warp<ST, T, B>(), G::NS>;
+    using G = TileOf<ST, T, B, NW>;
+    return stencil3d_tile_kernel<ST, T, B, NW, rows_per_warp<ST, T, B>(), G::NS>;
   } else {
     return stencil3d_kernel<ST, T, B, FMA, kTj3D>;
   }
 }
 
-template <class ST, typename T, int B, bool FMA>
-constexpr int threads3d() { return use_tile3d<ST, FMA>() ? kNw3D * 32 : kTj3D * 32; }
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
+constexpr int threads3d() { return use_tile3d<ST, FMA>() ? NW * 32 : kTj3D * 32; }
 
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {
-  constexpr int NT = threads3d<ST, T, B, FMA>();
-  auto kern = kernel3d_ptr<ST, T, B, FMA>();
-  const size_t smem = smem_bytes3d<ST, T, B, FMA>();
+  constexpr int NT = threads3d<ST, T, B, FMA, NW>();
+  auto kern = kernel3d_ptr<ST, T, B, FMA, NW>();
+  const size_t smem = smem_bytes3d<ST, T, B, FMA, NW>();
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -768,7 +495,7 @@ cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {
   const bool fold = FMA && ST::kHasDiv;  // the divisor is nonzero (checked by the planner)
   const long long grid = (long long)a.ntk * a.ntj * a.nblocks;
   if constexpr (use_tile3d<ST, FMA>()) {
-    using G = TileOf<ST, T, B>;
+    using G = TileOf<ST, T, B, NW>;
     Params3T<T, ST::kTerms> p;
     cudaError_t e = encode_plane_map(&p.tmap, a.src, (int)sizeof(T), a.pitch, a.d1, a.d0, G::BX, G::BY);
     if (e != cudaSuccess) return e;
@@ -813,11 +540,11 @@ cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 int occupancy3d() {
-  constexpr int NT = threads3d<ST, T, B, FMA>();
-  auto kern = kernel3d_ptr<ST, T, B, FMA>();
-  const size_t smem = smem_bytes3d<ST, T, B, FMA>();
+  constexpr int NT = threads3d<ST, T, B, FMA, NW>();
+  auto kern = kernel3d_ptr<ST, T, B, FMA, NW>();
+  const size_t smem = smem_bytes3d<ST, T, B, FMA, NW>();
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     (void)cudaGetLastError();
     return 0;

@@ -1,4 +1,5 @@
-// Autotuner: chooses (bt, sl) per (stencil, dtype, fp mode, grid size class).
+// Autotuner: chooses (bt, sl, bs1) per (stencil, dtype, fp mode, grid size
+// class); bs1 is the 3-D tile's rows (the block shape), 0 in 2-D.
 //
 // Replaces the artifact's offline performance model (Model_V100.xlsm, sheets
 // Formula / Macro, whose top configuration per stencil is listed in
@@ -16,8 +17,9 @@
 // stencil, dtype and mode, else the engine's fixed rule.
 //
 // Table file: one entry per line, '#' starts a comment:
-//   <stencil> <f32|f64> <exact|fma> <size class> <bt> <sl> <ms per step>
-// where the size class is floor(log2(interior cells)).
+//   <stencil> <f32|f64> <exact|fma> <size class> <bt> <sl> [<bs1>] <ms per step>
+// where the size class is floor(log2(interior cells)) and bs1 (3-D tile
+// rows; 0 or absent: the launcher's default shape) is optional.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,6 +40,7 @@ namespace {
 struct Entry {
   int sid, dtype, fma, cls, bt, sl;
   double ms;
+  int bs1;
 };
 
 std::mutex g_mu;
@@ -63,11 +66,17 @@ gbs_status load_locked(const char *path) {
     if (hash) *hash = 0;
     char name[64], dt[8], mode[8];
     Entry e{};
-    const int k = std::sscanf(line, "%63s %7s %7s %d %d %d %lf", name, dt, mode, &e.cls, &e.bt, &e.sl, &e.ms);
+    double f7 = 0.0, f8 = 0.0;
+    const int k = std::sscanf(line, "%63s %7s %7s %d %d %d %lf %lf", name, dt, mode, &e.cls, &e.bt, &e.sl, &f7, &f8);
     if (k <= 0) continue;
-    if (k != 7) {
+    if (k == 7) {
+      e.ms = f7;
+    } else if (k == 8 && f7 == (double)(int)f7 && f7 >= 0) {
+      e.bs1 = (int)f7;
+      e.ms = f8;
+    } else {
       std::fclose(f);
-      return fail(GBS_ERR_INVALID, "%s:%d: expected 7 fields", path, lineno);
+      return fail(GBS_ERR_INVALID, "%s:%d: expected 7 or 8 fields", path, lineno);
     }
     e.sid = gbs_stencil_id(name);
     e.dtype = !std::strcmp(dt, "f32") ? GBS_F32 : !std::strcmp(dt, "f64") ? GBS_F64 : -1;
@@ -127,12 +136,13 @@ double fp_flops_per_s(int dtype) {
   return cached[k];
 }
 
-// redundancy (computed cells / useful cells) of (bt, sl) for d, as gbs_plan
-// reports it; < 0 if the geometry is invalid
-double redundancy(const gbs_desc *d, int bt, int sl) {
+// redundancy (computed cells / useful cells) of (bt, sl, bs1) for d, as
+// gbs_plan reports it; < 0 if the geometry is invalid
+double redundancy(const gbs_desc *d, int bt, int sl, int bs1) {
   gbs_desc c = *d;
   c.bt = bt;
   c.sl = sl;
+  c.bs1 = bs1;
   gbs_plan_info pi;
   if (gbs_plan(&c, &pi) != GBS_OK) return -1.0;
   return pi.redundancy;
@@ -141,7 +151,7 @@ double redundancy(const gbs_desc *d, int bt, int sl) {
 }  // namespace
 
 // The table's choice for d, if any (bt = 0 otherwise); used by the run path.
-bool tuned_lookup(const gbs_desc *d, int *bt, int *sl) {
+bool tuned_lookup(const gbs_desc *d, int *bt, int *sl, int *bs1) {
   std::lock_guard<std::mutex> lk(g_mu);
   env_load_locked();
   const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
@@ -155,6 +165,7 @@ bool tuned_lookup(const gbs_desc *d, int *bt, int *sl) {
   if (!best || std::abs(best->cls - cls) > 3) return false;
   *bt = best->bt;
   *sl = best->cls == cls ? best->sl : 0;  // stream length only for the exact size class
+  if (bs1) *bs1 = best->bs1;
   return true;
 }
 
@@ -176,14 +187,14 @@ gbs_status gbs_tune_save(const char *path) {
   std::lock_guard<std::mutex> lk(g_mu);
   FILE *f = std::fopen(path, "w");
   if (!f) return fail(GBS_ERR_INVALID, "cannot write %s", path);
-  std::fprintf(f, "# stencil dtype mode size_class bt sl ms_per_step\n");
+  std::fprintf(f, "# stencil dtype mode size_class bt sl bs1 ms_per_step\n");
   std::vector<Entry> t = g_table;
   std::sort(t.begin(), t.end(), [](const Entry &a, const Entry &b) {
     return std::make_tuple(a.sid, a.dtype, a.fma, a.cls) < std::make_tuple(b.sid, b.dtype, b.fma, b.cls);
   });
   for (const Entry &e : t)
-    std::fprintf(f, "%s %s %s %d %d %d %.6g\n", gbs_stencil_name(e.sid), e.dtype == GBS_F64 ? "f64" : "f32",
-                 e.fma ? "fma" : "exact", e.cls, e.bt, e.sl, e.ms);
+    std::fprintf(f, "%s %s %s %d %d %d %d %.6g\n", gbs_stencil_name(e.sid), e.dtype == GBS_F64 ? "f64" : "f32",
+                 e.fma ? "fma" : "exact", e.cls, e.bt, e.sl, e.bs1, e.ms);
   std::fclose(f);
   return GBS_OK;
 }
@@ -207,9 +218,14 @@ gbs_status gbs_tune_set(const gbs_desc *d, int bt, int sl, double ms_per_step) {
   const int mx = max_bt(d->stencil, d->dtype, fma);
   if (bt < 1 || bt > mx) return fail(GBS_ERR_INVALID, "bt=%d outside 1..%d", bt, mx);
   if (sl < 0) return fail(GBS_ERR_INVALID, "sl < 0");
+  if (stencil_def(d->stencil)->dim == 3 && d->bs1 > 0) {
+    gbs_desc t = *d;
+    t.bt = bt;
+    if (variant_3d(&t, bt) < 0) return GBS_ERR_UNSUPPORTED;
+  }
   std::lock_guard<std::mutex> lk(g_mu);
   env_load_locked();
-  record_locked(Entry{d->stencil, d->dtype, fma, size_class(d), bt, sl, ms_per_step});
+  record_locked(Entry{d->stencil, d->dtype, fma, size_class(d), bt, sl, ms_per_step, std::max(0, d->bs1)});
   return GBS_OK;
 }
 
@@ -219,7 +235,7 @@ gbs_status gbs_tune_lookup(const gbs_desc *d, int *bt, int *sl) {
   if (!bt || !sl) return fail(GBS_ERR_INVALID, "NULL output");
   *bt = 0;
   *sl = 0;
-  tuned_lookup(d, bt, sl);
+  tuned_lookup(d, bt, sl, nullptr);
   return GBS_OK;
 }
 
@@ -262,18 +278,30 @@ gbs_status gbs_tune(const gbs_desc *d, gbs_tune_candidate *cands, int max_cands,
   const int nsl = s->dim == 2 ? 5 : 4;
   const int axis0 = d->n[0];
   for (int bt = 1; bt <= mx; ++bt) {
-    for (int k = 0; k < nsl; ++k) {
-      if (sls[k] != 0 && sls[k] >= axis0) continue;
-      const double red = redundancy(d, bt, sls[k]);
-      if (red <= 0.0) continue;
-      const double per_cell = std::max(2.0 * S / (bt * B), red * s->fpp / P);
-      gbs_tune_candidate c{};
-      c.bt = bt;
-      c.sl = sls[k];
-      c.redundancy = red;
-      c.model_ms_per_step = (cells * per_cell + launch_gap_s / bt) * 1e3;
-      c.ms_per_step = -1.0;
-      cs.push_back(c);
+    // block shapes: the 3-D launcher's built tile heights, else the one shape
+    std::vector<int> shapes{0};
+    if (s->dim == 3) {
+      shapes.clear();
+      for (int v = 0; v < kVar3; ++v) {
+        const Tile3DShape ts = tile_shape_3d(d->stencil, d->dtype, fma, bt, v);
+        if (ts.tj > 0) shapes.push_back(ts.tj);
+      }
+    }
+    for (int bs1 : shapes) {
+      for (int k = 0; k < nsl; ++k) {
+        if (sls[k] != 0 && sls[k] >= axis0) continue;
+        const double red = redundancy(d, bt, sls[k], bs1);
+        if (red <= 0.0) continue;
+        const double per_cell = std::max(2.0 * S / (bt * B), red * s->fpp / P);
+        gbs_tune_candidate c{};
+        c.bt = bt;
+        c.sl = sls[k];
+        c.bs1 = bs1;
+        c.redundancy = red;
+        c.model_ms_per_step = (cells * per_cell + launch_gap_s / bt) * 1e3;
+        c.ms_per_step = -1.0;
+        cs.push_back(c);
+      }
     }
   }
   if (cs.empty()) return fail(GBS_ERR_UNSUPPORTED, "no valid (bt, sl) for %s at this size", s->name);
@@ -317,6 +345,7 @@ gbs_status gbs_tune(const gbs_desc *d, gbs_tune_candidate *cands, int max_cands,
     gbs_desc t = *d;
     t.bt = c.bt;
     t.sl = c.sl;
+    t.bs1 = c.bs1;
     // full-degree launches only: T a multiple of 2*bt, about 4 ms of work
     const int reps = (int)std::min(64.0, std::max(1.0, std::ceil(4.0 / (c.model_ms_per_step * 2 * c.bt))));
     t.timestep = 2 * c.bt;
@@ -359,7 +388,8 @@ gbs_status gbs_tune(const gbs_desc *d, gbs_tune_candidate *cands, int max_cands,
   {
     std::lock_guard<std::mutex> lk(g_mu);
     env_load_locked();
-    record_locked(Entry{d->stencil, d->dtype, fma, size_class(d), cs[0].bt, cs[0].sl, cs[0].ms_per_step});
+    record_locked(Entry{d->stencil, d->dtype, fma, size_class(d), cs[0].bt, cs[0].sl, cs[0].ms_per_step,
+                        cs[0].bs1});
   }
   if (ncands) *ncands = (int)cs.size();
   for (int i = 0; i < max_cands && i < (int)cs.size(); ++i) cands[i] = cs[i];

@@ -54,7 +54,7 @@ class PlanInfo(ctypes.Structure):
 
 
 class BatchGrid(ctypes.Structure):
-    _fields_ = [("stencil", ctypes.c_int), ("n", ctypes.c_int * 2), ("timestep", ctypes.c_int),
+    _fields_ = [("stencil", ctypes.c_int), ("n", ctypes.c_int * 3), ("timestep", ctypes.c_int),
                 ("dev_A", ctypes.c_void_p), ("coef", ctypes.c_void_p), ("divisor", ctypes.c_double)]
 
 
@@ -91,6 +91,20 @@ SIGNATURES = [
                                            ctypes.c_void_p]),
     ("gbs_adjoint_backward", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gbs_adjoint_workspace_slots", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.c_int,
+                                                   ctypes.POINTER(ctypes.c_size_t)]),
+    ("gbs_adjoint_backward_slots", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
+    ("gbs_adjoint_plan_budget", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_size_t, ctypes.POINTER(ctypes.c_int),
+                                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_size_t)]),
+    ("gbs_revolve_cost", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
+                                        ctypes.POINTER(ctypes.c_int)]),
+    ("gbs_adjoint_forward_batch", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                                 ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p]),
+    ("gbs_adjoint_backward_batch", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                                  ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                                  ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p]),
     ("gbs_measure_fp_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gbs_tune", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     ("gbs_tune_set", ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.c_int, ctypes.c_double]),
@@ -220,22 +234,17 @@ class Batch:
     MODES = {"persistent": 0, "layered": 1, "streams": 2}
 
     def __init__(self, grids, fp_mode="fma", mode="persistent"):
-        """grids: list of (DeviceGrid-like with .name, .n, .buf, timestep, coef or None)."""
-        arr = (BatchGrid * len(grids))()
+        """grids: list of (DeviceGrid-like with .name, .n, .dtype, .buf, timestep, coef or None),
+        all of one dtype."""
+        dts = {np.dtype(getattr(g, "dtype", np.float32)) for g, _, _ in grids}
+        if len(dts) != 1:
+            raise ValueError("a batch holds grids of one dtype")
+        dt = dts.pop()
         self._keep = []
-        for i, (g, T, coef) in enumerate(grids):
-            arr[i].stencil = stencil_id(g.name)
-            arr[i].n[0], arr[i].n[1] = int(g.n[0]), int(g.n[1])
-            arr[i].timestep = int(T)
-            arr[i].dev_A = g.buf.data_ptr()
-            if coef is not None:
-                c = np.ascontiguousarray(coef, dtype=np.float32)
-                self._keep.append(c)
-                arr[i].coef = c.ctypes.data
-            arr[i].divisor = 0.0
+        arr = _batch_grids(grids, dt, self._keep)
         h = ctypes.c_void_p()
-        check(lib().gbs_batch_plan(arr, len(grids), GBS_F32, FP_MODES[fp_mode], self.MODES[mode],
-                                   ctypes.byref(h)))
+        check(lib().gbs_batch_plan(arr, len(grids), GBS_F32 if dt == np.float32 else GBS_F64,
+                                   FP_MODES[fp_mode], self.MODES[mode], ctypes.byref(h)))
         self.handle = h
 
     def run(self, stream: int = 0):
@@ -258,20 +267,29 @@ class Batch:
             pass
 
 
-def batch_run_noalloc(grids, fp_mode="fma", stream: int = 0):
-    """gbs_batch_run_noalloc over (DeviceGrid, timestep, coef or None)
-    entries: the batched run that allocates no memory itself."""
+def _batch_grids(grids, dtype, keep):
+    """gbs_batch_grid entries for (grid, timestep, coef or None) tuples;
+    coefficient arrays are appended to ``keep``."""
     arr = (BatchGrid * len(grids))()
-    keep = []
     for i, (g, T, coef) in enumerate(grids):
         arr[i].stencil = stencil_id(g.name)
-        arr[i].n[0], arr[i].n[1] = int(g.n[0]), int(g.n[1])
+        for a in range(3):
+            arr[i].n[a] = int(g.n[a]) if a < len(g.n) else 1
         arr[i].timestep = int(T)
         arr[i].dev_A = g.buf.data_ptr()
         if coef is not None:
-            c = np.ascontiguousarray(coef, dtype=np.float32)
+            c = np.ascontiguousarray(coef, dtype=dtype)
             keep.append(c)
             arr[i].coef = c.ctypes.data
+        arr[i].divisor = 0.0
+    return arr
+
+
+def batch_run_noalloc(grids, fp_mode="fma", stream: int = 0):
+    """gbs_batch_run_noalloc over (DeviceGrid, timestep, coef or None)
+    entries: the batched run that allocates no memory itself."""
+    keep = []
+    arr = _batch_grids(grids, np.float32, keep)
     check(lib().gbs_batch_run_noalloc(arr, len(grids), FP_MODES[fp_mode], ctypes.c_void_p(stream)))
 
 

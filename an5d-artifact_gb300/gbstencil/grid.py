@@ -44,8 +44,8 @@ class DeviceGrid:
             v = flat.view(L.dimsize[0], L.dimsize[1], L.pitch)
         return v[..., L.shift:L.shift + L.dimsize[self.dim - 1]]
 
-    def desc(self, timestep, fp_mode="fma", bt=0, sl=0, coef=None, divisor=0.0, eps=0.0):
-        return capi.make_desc(self.name, self.dtype, self.n, timestep, fp_mode, bt, sl,
+    def desc(self, timestep, fp_mode="fma", bt=0, sl=0, coef=None, divisor=0.0, eps=0.0, bs1=0):
+        return capi.make_desc(self.name, self.dtype, self.n, timestep, fp_mode, bt, sl, bs1=bs1,
                               coef=coef, divisor=divisor, eps=eps)
 
     def upload(self, host: np.ndarray, stream: int | None = None):
@@ -73,9 +73,9 @@ class DeviceGrid:
         self.plane(1).copy_(p0)
 
     def run(self, timestep: int, fp_mode="fma", bt=0, sl=0, coef=None, divisor=0.0, eps=0.0,
-            stream: int | None = None):
+            stream: int | None = None, bs1=0):
         """Enqueues the time loop on ``stream`` (default: torch's current)."""
-        d, keep = self.desc(timestep, fp_mode, bt, sl, coef, divisor, eps)
+        d, keep = self.desc(timestep, fp_mode, bt, sl, coef, divisor, eps, bs1)
         s = torch.cuda.current_stream(self.device).cuda_stream if stream is None else stream
         capi.run_device(d, self.buf.data_ptr(), s)
         return keep

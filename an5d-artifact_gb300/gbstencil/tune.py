@@ -24,7 +24,7 @@ DEFAULT_TABLE = Path(__file__).resolve().parent / "tuning_gb300.txt"
 
 class Candidate(ctypes.Structure):
     _fields_ = [("bt", ctypes.c_int), ("sl", ctypes.c_int), ("redundancy", ctypes.c_double),
-                ("model_ms_per_step", ctypes.c_double), ("ms_per_step", ctypes.c_double)]
+                ("model_ms_per_step", ctypes.c_double), ("ms_per_step", ctypes.c_double), ("bs1", ctypes.c_int)]
 
 
 def tune(name: str, dtype, n, fp_mode="fma", max_cands: int = 64):
@@ -34,8 +34,9 @@ def tune(name: str, dtype, n, fp_mode="fma", max_cands: int = 64):
     buf = (Candidate * max_cands)()
     nc = ctypes.c_int(0)
     capi.check(capi.lib().gbs_tune(ctypes.byref(d), ctypes.cast(buf, ctypes.c_void_p), max_cands, ctypes.byref(nc)))
-    out = [{"bt": c.bt, "sl": c.sl, "redundancy": c.redundancy, "model_ms_per_step": c.model_ms_per_step,
-            "ms_per_step": c.ms_per_step} for c in buf[:min(nc.value, max_cands)]]
+    out = [{"bt": c.bt, "sl": c.sl, "bs1": c.bs1, "redundancy": c.redundancy,
+            "model_ms_per_step": c.model_ms_per_step, "ms_per_step": c.ms_per_step}
+           for c in buf[:min(nc.value, max_cands)]]
     return out[0], out
 
 

@@ -73,8 +73,8 @@ BATCH_MIX = ["star2d1r", "star2d2r", "star2d3r", "star2d4r", "box2d1r", "box2d2r
 # once, so traffic grows in proportion). Keyed by (stencil, dtype, bt); the
 # value names the capture, whose summary is under profiles/.
 NCU_DRAM_BYTES_PER_CELL = {
-    ("box3d1r", "float64", 1): (15.74, "profiles/stencil3d_rows_box3d1r_f64_n256.md (256^3 capture)"),
-    ("star3d2r", "float32", 1): (8.20, "profiles/stencil3d_rows_star3d2r_f32_n320.md (320^3 capture)"),
+    ("box3d1r", "float64", 1): (14.80, "profiles/stencil3d_tile_box3d1r_f64_n256.md (256^3 capture)"),
+    ("star3d2r", "float32", 1): (9.01, "profiles/stencil3d_tile_star3d2r_f32_n320.md (320^3 capture)"),
 }
 
 
@@ -207,7 +207,7 @@ def run_ours(args, rank, world):
         g = DeviceGrid(name, dt, n, device=dev)
         g.fill_uniform(seed=20250101 + i)
         c = random_coefficients(name, dt, 1000 + i)
-        d, keep = g.desc(T, args.fp_mode, args.bt, 0, coef=c)
+        d, keep = g.desc(T, args.fp_mode, args.bt, 0, coef=c, bs1=args.bs1)
         plans.append(capi.plan(d))
         grids.append(g)
         coefs.append(c)
@@ -217,7 +217,7 @@ def run_ours(args, rank, world):
 
     def step():
         for g, c, (_, _, _, T) in zip(grids, coefs, work):
-            g.run(T, args.fp_mode, args.bt, 0, coef=c)
+            g.run(T, args.fp_mode, args.bt, 0, coef=c, bs1=args.bs1)
 
     for _ in range(args.warmup):
         step()
@@ -235,7 +235,7 @@ def run_ours(args, rank, world):
             flush.fill_(1.0)
             for gi, (g, c, (_, _, _, T)) in enumerate(zip(grids, coefs, work)):
                 ev[gi][0].record(stream)
-                g.run(T, args.fp_mode, args.bt, 0, coef=c)
+                g.run(T, args.fp_mode, args.bt, 0, coef=c, bs1=args.bs1)
                 ev[gi][1].record(stream)
             torch.cuda.synchronize()
             for gi in range(len(grids)):
@@ -255,7 +255,7 @@ def run_ours(args, rank, world):
     def e2e_step():
         nonlocal h2d, d2h
         for g, h, c, (_, _, _, T) in zip(grids, hosts, coefs, work):
-            d, keep = capi.make_desc(g.name, g.dtype, g.n, T, args.fp_mode, bt=args.bt, coef=c)
+            d, keep = capi.make_desc(g.name, g.dtype, g.n, T, args.fp_mode, bt=args.bt, bs1=args.bs1, coef=c)
             capi.run_host(d, h.numpy())
     e2e_samples = []
     if not args.no_e2e:
@@ -279,7 +279,7 @@ def run_ours(args, rank, world):
             Tc = 2 * p.bt if p.bt > 1 else 4
             g.fill_uniform(seed=20250101 + i)
             A = g.download()
-            g.run(Tc, args.fp_mode, p.bt, 0, coef=c)
+            g.run(Tc, args.fp_mode, p.bt, 0, coef=c, bs1=p.bs1 if args.bs1 else 0)
             capi.sync(stream.cuda_stream)
             got = g.download()
             po.run(g.name, A, g.n, Tc, coef=c)
@@ -489,7 +489,7 @@ def run_batched(args, rank, world):
     # the same work as per-grid plain launches, one grid after another
     def plain():
         for g, T, c in entries:
-            g.run(T, args.fp_mode, args.bt, 0, coef=c)
+            g.run(T, args.fp_mode, args.bt, 0, coef=c, bs1=args.bs1)
     plain()
     capi.sync(stream.cuda_stream)
     torch.cuda.synchronize()
@@ -551,14 +551,16 @@ def run_batched(args, rank, world):
     return line
 
 
-# The adjoint cases: (stencil, dtype, interior, T, checkpoint interval, loss,
-# coefficient gradients wanted)
+# The adjoint cases: (stencil, dtype, interior, T, checkpoint interval (or
+# a workspace budget in bytes, as "16GB"), loss, coefficient gradients wanted)
 ADJOINT_CASES = [
     ("j2d5pt", np.float32, [2048, 2048], 1024, 32, "half_sq_err", True),
-    ("gradient2d", np.float64, [4096, 4096], 512, 32, "mean_sq", False),
+    ("gradient2d", np.float64, [4096, 4096], 512, "16GB", "mean_sq", False),
     ("j3d27pt", np.float32, [384, 384, 384], 256, 16, "half_sq", False),
 ] + [("j3d27pt", np.float32, [n, n, n], 256, 16, "half_sq", False)
      for n in (192, 224, 256, 288, 320, 336, 352, 384)]
+# the uneven j3d27pt instances, also run as one batch
+BATCH_ADJOINT = [c for c in ADJOINT_CASES[3:]]
 
 
 def run_adjoint(args, rank, world):
@@ -581,7 +583,7 @@ def run_adjoint(args, rank, world):
         keep = {tuple(x.split(":")) for x in args.only.split(",")}
         todo = [c for c in todo if (c[0], np.dtype(c[1]).name) in keep][:1]
     if args.T:
-        todo = [(a, b, c, args.T, min(e, args.T), f, g) for a, b, c, d, e, f, g in todo]
+        todo = [(a, b, c, args.T, e if isinstance(e, str) else min(e, args.T), f, g) for a, b, c, d, e, f, g in todo]
     for ci, (name, dt, n, T, C, loss, want_coef) in enumerate(todo):
         tdt = torch.float32 if dt == np.float32 else torch.float64
         s = capi.info(name)
@@ -614,13 +616,15 @@ def run_adjoint(args, rank, world):
         capi.sync(stream.cuda_stream)
         plain = capi.plan(g.desc(T)[0])
         del g
-        run = Checkpointed(name, u0, T, C)
+        ckw = dict(checkpoint_every=C) if not isinstance(C, str) else dict(budget_bytes=int(float(C[:-2]) * 1e9))
+        run = Checkpointed(name, u0, T, **ckw)
         lam = lam_of(run.u_T)
+        C, slots, ws_bytes = run.checkpoint_every, run.slots, run.workspace_bytes
         bwd, ck = [], []
         for k in range(args.warmup + args.steps):
             flush.fill_(1.0)
             e0.record(stream)
-            run = Checkpointed(name, u0, T, C)
+            run = Checkpointed(name, u0, T, C, slots=slots)
             e1.record(stream)
             torch.cuda.synchronize()
             ck_ms = e0.elapsed_time(e1)
@@ -640,7 +644,7 @@ def run_adjoint(args, rank, world):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             du0 = hu0.to(dev, non_blocking=True)
-            run = Checkpointed(name, du0, T, C)
+            run = Checkpointed(name, du0, T, C, slots=slots)
             gu, gc = run.backward(lam_of(run.u_T), want_coef=want_coef)
             hgrad.copy_(gu, non_blocking=True)
             torch.cuda.synchronize()
@@ -664,10 +668,53 @@ def run_adjoint(args, rank, world):
         tot_cells += cells
         tot_bwd += b_ms
         cases.append({"stencil": name, "dtype": np.dtype(dt).name, "n": n, "T": T, "checkpoint_every": C,
+                      "stash_slots": slots, "schedule": "two-level" if slots >= 2 * C else "binomial",
+                      "workspace_bytes": ws_bytes,
                       "loss": loss, "coef_grad": want_coef, "forward_ms": round(f_ms, 3),
                       "forward_bt": plain.bt, "forward_checkpointed_ms": round(c_ms, 3),
                       "backward_ms": round(b_ms, 3), "backward_vs_forward": round(b_ms / f_ms, 3),
                       "backward_gcells_s": round(cells / (b_ms * 1e-3) / 1e9, 2)})
+    # the uneven instances as one batch (gbs_adjoint_forward_batch /
+    # gbs_adjoint_backward_batch) against the same instances one at a time
+    batch = None
+    bnames = [(c[0], c[2], c[3], c[4]) for c in BATCH_ADJOINT]
+    if not args.only and not args.T:
+        from gbstencil.adjoint import backward_batch, forward_batch
+        u0s, lams = [], []
+        for i, (name, n, T, C) in enumerate(bnames):
+            gen.manual_seed(777 + i)
+            shape = [x + 2 * capi.info(name)["rad"] for x in n]
+            u0s.append(torch.rand(shape, generator=gen, dtype=torch.float32, device=dev))
+        fw, bw = [], []
+        for k in range(args.warmup + args.steps):
+            flush.fill_(1.0)
+            e0.record(stream)
+            runs = forward_batch([(nm, u) for (nm, _, _, _), u in zip(bnames, u0s)], bnames[0][2], bnames[0][3])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            f_ms = e0.elapsed_time(e1)
+            lams = [r.u_T.clone() for r in runs]
+            flush.fill_(1.0)
+            e0.record(stream)
+            backward_batch(runs, lams)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                fw.append(f_ms)
+                bw.append(e0.elapsed_time(e1))
+            del runs
+        capi.sync(stream.cuda_stream)
+        one = {(c["stencil"], tuple(c["n"])): c for c in cases}
+        sum_b = sum(one[(nm, tuple(n))]["backward_ms"] for nm, n, _, _ in bnames if (nm, tuple(n)) in one)
+        sum_f = sum(one[(nm, tuple(n))]["forward_checkpointed_ms"] for nm, n, _, _ in bnames
+                    if (nm, tuple(n)) in one)
+        batch = {"instances": [f"{nm} {'x'.join(map(str, n))} T={T}" for nm, n, T, _ in bnames],
+                 "forward_checkpointed_ms": round(statistics.median(fw), 3),
+                 "backward_ms": round(statistics.median(bw), 3),
+                 "one_at_a_time_forward_checkpointed_ms": round(sum_f, 3),
+                 "one_at_a_time_backward_ms": round(sum_b, 3),
+                 "backward_speedup": round(sum_b / statistics.median(bw), 3)}
+        torch.cuda.empty_cache()
     tot_bwd = max_over_ranks(tot_bwd, world, dev)
     value = tot_cells * world / (tot_bwd * 1e-3) / 1e9
     hbm, peak_kind = load_peaks()
@@ -688,6 +735,7 @@ def run_adjoint(args, rank, world):
                                                      f"T={c['T']} C={c['checkpoint_every']}" for c in cases],
                    "l2": "flushed between timed runs (512 MB write)", "parallelism": "replicas" if world > 1 else "single GPU"},
         "adjoint": cases,
+        "adjoint_batch": batch,
         "e2e": None if args.no_e2e else {
             "value": round(tot_cells / (tot_e2e * 1e-3) / 1e9, 3), "unit": "GCells/s (forward+backward, host buffers)",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -729,6 +777,7 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=0, help="interior side length override")
     ap.add_argument("--T", type=int, default=0, help="timestep override")
     ap.add_argument("--bt", type=int, default=0, help="fused degree of every grid (0: the tuned one)")
+    ap.add_argument("--bs1", type=int, default=0, help="3-D tile rows of every grid (0: the tuned shape)")
     ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
     ap.add_argument("--batch-mode", default="streams", choices=["persistent", "layered", "streams"],

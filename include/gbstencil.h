@@ -64,8 +64,12 @@ typedef struct gbs_desc {
   int timestep;      /* T >= 0 */
   int fp_mode;       /* GBS_FP_EXACT | GBS_FP_FMA */
   int bt;            /* timesteps fused per launch (temporal degree); 0 = tuned */
-  int bs1;           /* 2-D: warps per CTA; 3-D: tile rows (warps) per CTA; 0 = tuned */
-  int bs2;           /* reserved for the 3-D tile width; 0 */
+  int bs1;           /* block shape. 3-D (FMA mode): tile rows per CTA, one of
+                        the heights built for the degree (gbs_plan reports
+                        them; 64 and 32 rows for most stencils at bt=1);
+                        2-D: warps per CTA, 4; 0 = tuned */
+  int bs2;           /* tile columns: 32 * (16 bytes / element size) (one
+                        warp's 16-byte vector per lane); 0 = that */
   int sl;            /* stream block length in rows (2-D) / planes (3-D); 0 = tuned */
   const void *coef;  /* NULL: the source literals. Else nterms values of dtype,
                         term order as in the source (the gradient form takes
@@ -138,12 +142,14 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out);
  * floor(log2(interior cells)), is nearest, within 3), else by a fixed rule.
  * The table is also loaded from the file named by the environment variable
  * GBS_TUNING at first use. Text format, one entry per line:
- * "<stencil> <f32|f64> <exact|fma> <size class> <bt> <sl> <ms per step>". */
+ * "<stencil> <f32|f64> <exact|fma> <size class> <bt> <sl> [<bs1>] <ms per step>"
+ * (bs1: 3-D tile rows; absent or 0: the default shape). */
 typedef struct gbs_tune_candidate {
   int bt, sl;               /* sl 0: the engine's one-wave stream length */
   double redundancy;        /* computed / useful cells per launch */
   double model_ms_per_step; /* the model's time for one timestep */
   double ms_per_step;       /* measured; < 0 if the model pruned it */
+  int bs1;                  /* 3-D tile rows (block shape); 0 in 2-D */
 } gbs_tune_candidate;
 gbs_status gbs_tune(const gbs_desc *d, gbs_tune_candidate *cands, int max_cands, int *ncands);
 gbs_status gbs_tune_set(const gbs_desc *d, int bt, int sl, double ms_per_step);
@@ -163,18 +169,20 @@ gbs_status gbs_download(const gbs_desc *d, const void *dev_A, void *host_A, void
  * gave up) into GBS_ERR_TIMEOUT. */
 gbs_status gbs_sync(void *stream);
 
-/* ---- batched persistent launch ---------------------------------------- */
-/* Many independent 2-D grids (any mix of the 2-D stencils, sizes and step
- * counts), advanced by ONE persistent kernel launch captured in a CUDA graph.
- * No counterpart in the artifact, which runs one grid per process; this
- * replaces a loop of per-grid kernel_stencil calls. */
+/* ---- batched launch ------------------------------------------------------ */
+/* Many independent grids (any mix of stencils, sizes and step counts),
+ * advanced by ONE launch of a CUDA graph. No counterpart in the artifact,
+ * which runs one grid per process; this replaces a loop of per-grid
+ * kernel_stencil calls. */
 typedef struct gbs_batch_grid {
-  int stencil;        /* a 2-D stencil id */
-  int n[2];           /* interior extent per axis */
+  int stencil;        /* a stencil id (3-D stencils: GBS_BATCH_STREAMS only) */
+  int n[3];           /* interior extent per axis (n[2] ignored for 2-D) */
   int timestep;       /* T >= 0 */
   void *dev_A;        /* two-plane grid in the engine layout (gbs_get_layout of
-                         the same stencil, GBS_F32 and n), 128-byte aligned */
-  const void *coef;   /* NULL = the source literals, else nterms floats */
+                         the same stencil, the batch's dtype and n), 128-byte
+                         aligned */
+  const void *coef;   /* NULL = the source literals, else nterms values of the
+                         batch's dtype */
   double divisor;     /* 0 = the source value */
 } gbs_batch_grid;
 
@@ -188,25 +196,27 @@ typedef struct gbs_batch_stats {
   int mode;                /* GBS_BATCH_PERSISTENT | GBS_BATCH_LAYERED | GBS_BATCH_STREAMS */
 } gbs_batch_stats;
 
-/* How a batch plan schedules its work items (grid, time block, strip,
- * stream block):
- * GBS_BATCH_PERSISTENT: one persistent kernel; warps take items in time-block
- *   order from an atomic counter and wait (bounded) on per-grid completion
- *   counters for the grid's previous time block.
- * GBS_BATCH_LAYERED: one kernel node per time block in the graph, each over
- *   every grid's items of that block; kernel boundaries order the blocks, so
- *   nothing waits on the device.
+/* How a batch plan schedules its work:
+ * GBS_BATCH_PERSISTENT: one persistent kernel over work items (grid, time
+ *   block, strip, stream block) of 2-D float grids; warps take items in
+ *   time-block order from an atomic counter and wait (bounded) on per-grid
+ *   completion counters for the grid's previous time block.
+ * GBS_BATCH_LAYERED: the same 2-D work items, one kernel node per time block
+ *   in the graph, each over every grid's items of that block; kernel
+ *   boundaries order the blocks, so nothing waits on the device.
  * GBS_BATCH_STREAMS: each grid's own time loop (the single-grid kernels at
  *   the tuned degree, one kernel node per fused launch) as a chain in the
  *   graph; the chains are spread over 16 branches (environment
  *   GBS_BATCH_BRANCHES, 1..64), heaviest grid first onto the least loaded
- *   branch, so independent grids run side by side. */
+ *   branch, so independent grids run side by side. Takes 2-D and 3-D grids,
+ *   float or double. */
 enum { GBS_BATCH_PERSISTENT = 0, GBS_BATCH_LAYERED = 1, GBS_BATCH_STREAMS = 2 };
 
-/* Plans the batch: work items, per-grid dependency counters and the CUDA
- * graph (counter reset + the persistent kernel). Allocates device memory
- * owned by the plan. dtype must be GBS_F32. The grids' buffers must stay
- * valid while the plan is used. */
+/* Plans the batch: the CUDA graph, and for the work-item schedules the work
+ * list and per-grid dependency counters (device memory owned by the plan).
+ * dtype: GBS_F32 for every schedule, GBS_F64 for GBS_BATCH_STREAMS; a 3-D
+ * grid or GBS_F64 under a work-item schedule is GBS_ERR_UNSUPPORTED. The
+ * grids' buffers must stay valid while the plan is used. */
 gbs_status gbs_batch_plan(const gbs_batch_grid *grids, int ngrids, int dtype, int fp_mode, int mode,
                           gbs_batch **out);
 /* Replays the plan's graph on `stream` (asynchronous; see gbs_sync). */
@@ -257,6 +267,41 @@ gbs_status gbs_adjoint_forward(const gbs_desc *d, void *dev_A, int checkpoint_ev
                                void *stream);
 gbs_status gbs_adjoint_backward(const gbs_desc *d, const void *dev_lamT, void *dev_grad_u0, double *dev_coef_grad,
                                 int checkpoint_every, void *workspace, void *stream);
+
+/* The same backward under a smaller memory budget: the workspace holds
+ * `slots` stash planes instead of 2C. With slots >= 2C this is
+ * gbs_adjoint_backward; with fewer, each chunk of C steps is reversed by the
+ * binomial (revolve) checkpoint schedule over `slots` snapshot planes (plus
+ * two work planes), which recomputes the fewest forward steps any schedule
+ * with that many snapshots can (slots = 0: every state recomputed from the
+ * chunk's checkpoint). gbs_adjoint_forward is the same for both; the
+ * workspace must be sized by gbs_adjoint_workspace_slots with the same C
+ * and slots. */
+gbs_status gbs_adjoint_workspace_slots(const gbs_desc *d, int checkpoint_every, int slots, size_t *bytes);
+gbs_status gbs_adjoint_backward_slots(const gbs_desc *d, const void *dev_lamT, void *dev_grad_u0,
+                                      double *dev_coef_grad, int checkpoint_every, int slots, void *workspace,
+                                      void *stream);
+/* Chooses C and slots for a workspace of at most budget_bytes: the fewest
+ * recomputed forward steps (ties: the smaller workspace). GBS_ERR_NOMEM if
+ * nothing fits. Host arithmetic only. */
+gbs_status gbs_adjoint_plan_budget(const gbs_desc *d, size_t budget_bytes, int *checkpoint_every, int *slots,
+                                   size_t *bytes);
+/* Forward steps the binomial schedule takes to reverse `steps` steps with
+ * `slots` snapshot planes, and the most snapshots it holds at once. Host
+ * arithmetic only. */
+gbs_status gbs_revolve_cost(int steps, int slots, long long *forward_steps, int *peak_slots);
+
+/* Many independent instances (any mix of stencils, sizes and dtypes, one
+ * workspace each) at once: the instances' forward (or backward) calls run
+ * side by side on internal branch streams, forked from `stream` and joined
+ * back into it, so the calls are asynchronous on `stream` like the
+ * single-instance ones. dev_coef_grad may be NULL (no coefficient gradients)
+ * or hold one pointer (or NULL) per instance. */
+gbs_status gbs_adjoint_forward_batch(const gbs_desc *descs, int n, void *const *dev_A, int checkpoint_every,
+                                     void *const *workspaces, void *stream);
+gbs_status gbs_adjoint_backward_batch(const gbs_desc *descs, int n, const void *const *dev_lamT,
+                                      void *const *dev_grad_u0, double *const *dev_coef_grad, int checkpoint_every,
+                                      void *const *workspaces, void *stream);
 
 /* Measures the device's fused multiply-add throughput in GFLOP/s (2 flops per
  * FMA): the FP term of the temporally-blocked stencil roofline. */

@@ -130,6 +130,84 @@ def test_adjoint_matches_reference_wide_rows(name, dtype, n, T, C, want_coef):
         assert gc is None
 
 
+REVOLVE_CASES = [
+    # name, dtype, n, T, checkpoint interval, snapshot slots (< 2C: binomial schedule)
+    ("j2d5pt", np.float32, 40, 37, 8, 0),
+    ("j2d5pt", np.float32, 40, 37, 8, 1),
+    ("j2d5pt", np.float64, 33, 37, 13, 3),
+    ("gradient2d", np.float64, 24, 20, 7, 2),
+    ("star3d1r", np.float64, 12, 9, 9, 1),
+    ("j3d27pt", np.float32, 11, 12, 12, 4),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,dtype,n,T,C,slots", REVOLVE_CASES, ids=lambda v: getattr(v, "__name__", str(v)))
+def test_adjoint_binomial_schedule_matches_reference(name, dtype, n, T, C, slots):
+    """A forced small budget: each chunk reversed by the revolve schedule."""
+    import torch
+    from gbstencil.adjoint import Checkpointed
+    u0, w = _inputs(name, n, 11)
+    u0 = u0.astype(dtype).astype(np.float64)
+    coef = ar.default_coef(name)
+    tdt = torch.float32 if dtype == np.float32 else torch.float64
+    run = Checkpointed(name, torch.tensor(u0, dtype=tdt, device="cuda"), T, C, slots=slots)
+    gu, gc = run.backward(torch.tensor(w, dtype=tdt, device="cuda"), want_coef=True)
+    full = Checkpointed(name, torch.tensor(u0, dtype=tdt, device="cuda"), T, C)
+    fu, fc = full.backward(torch.tensor(w, dtype=tdt, device="cuda"), want_coef=True)
+    torch.cuda.synchronize()
+    # the recomputed states are the forward's, bit for bit: the same result as the full stash
+    assert torch.equal(gu, fu) and torch.equal(gc, fc)
+    ref_gu, ref_gc = ar.adjoint(name, u0, coef, T, w)
+    tol = 1e-4 if dtype == np.float32 else 1e-9
+    assert _rel(gu.double().cpu().numpy(), ref_gu) <= tol
+    assert _rel(gc.cpu().numpy(), ref_gc) <= tol
+
+
+@pytest.mark.gpu
+def test_adjoint_budget_planner_run():
+    import torch
+    from gbstencil.adjoint import Checkpointed
+    name, n, T = "j2d5pt", 64, 40
+    u0, w = _inputs(name, n, 12)
+    t0 = torch.tensor(u0, device="cuda")
+    full = Checkpointed(name, t0, T, 8)
+    small = Checkpointed(name, t0, T, budget_bytes=full.workspace_bytes // 3)
+    assert small.workspace_bytes <= full.workspace_bytes // 3
+    a, ca = full.backward(torch.tensor(w, device="cuda"))
+    b, cb = small.backward(torch.tensor(w, device="cuda"))
+    ref_gu, ref_gc = ar.adjoint(name, u0, ar.default_coef(name), T, w)
+    assert _rel(b.cpu().numpy(), ref_gu) <= 1e-9 and _rel(cb.cpu().numpy(), ref_gc) <= 1e-9
+    assert _rel(a.cpu().numpy(), b.cpu().numpy()) <= 1e-13
+
+
+@pytest.mark.gpu
+def test_adjoint_batch_matches_single_instances():
+    """Uneven 3-D instances (and a 2-D one) at once through
+    gbs_adjoint_forward_batch / gbs_adjoint_backward_batch."""
+    import torch
+    from gbstencil.adjoint import Checkpointed, backward_batch, forward_batch
+    specs = [("j3d27pt", 10), ("j3d27pt", 14), ("j3d27pt", 17), ("star3d1r", 12)]
+    T, C = 9, 4
+    u0s, ws = [], []
+    for i, (name, n) in enumerate(specs):
+        u0, w = _inputs(name, n, 20 + i)
+        u0s.append(torch.tensor(u0, dtype=torch.float32, device="cuda"))
+        ws.append(torch.tensor(w, dtype=torch.float32, device="cuda"))
+    runs = forward_batch([(nm, u) for (nm, _), u in zip(specs, u0s)], T, C)
+    outs, _ = backward_batch(runs, ws)
+    outs_c, cgs = backward_batch(runs, ws, want_coef=True)
+    torch.cuda.synchronize()
+    for (name, n), u, w, r, g, gc2, g2 in zip(specs, u0s, ws, runs, outs, cgs, outs_c):
+        one = Checkpointed(name, u, T, C)
+        gu, gc = one.backward(w, want_coef=True)
+        torch.cuda.synchronize()
+        assert torch.equal(r.u_T, one.u_T)
+        assert torch.equal(g, gu) and torch.equal(g2, gu) and torch.equal(gc2, gc)
+        ref_gu, ref_gc = ar.adjoint(name, u.double().cpu().numpy(), ar.default_coef(name), T, w.double().cpu().numpy())
+        assert _rel(g.double().cpu().numpy(), ref_gu) <= 1e-4
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["j2d5pt", "gradient2d", "star3d1r"])
 def test_adjoint_directional_finite_difference(name):

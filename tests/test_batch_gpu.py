@@ -94,3 +94,48 @@ def test_batch_replay_matches_two_runs():
     po.run(name, ref, nn, 2 * T)
     assert np.array_equal(out[T % 2], ref[(2 * T) % 2])
     b.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_batch_3d_streams_matches_oracle(dtype):
+    """Uneven 3-D grids (j3d27pt as in the batched adjoint configuration,
+    with other 3-D stencils mixed in) in one graph launch of the streams
+    schedule: each grid as its own time loop, within the FMA tolerance of
+    the oracle."""
+    specs = [("j3d27pt", [19, 23, 40], 7), ("j3d27pt", [24, 24, 24], 10), ("j3d27pt", [31, 17, 66], 5),
+             ("star3d2r", [20, 30, 41], 6), ("box3d1r", [33, 12, 25], 9), ("star3d1r", [16, 16, 16], 0)]
+    tol = 1e-5 if dtype == np.float32 else 1e-12
+    grids, hosts, entries = [], [], []
+    for i, (name, n, T) in enumerate(specs):
+        shape, nn = po.grid_shape(name, n)
+        rng = np.random.default_rng(300 + i)
+        A = np.empty(shape, dtype)
+        A[0] = rng.random(shape[1:])
+        A[1] = A[0]
+        g = DeviceGrid(name, dtype, n)
+        g.upload(A)
+        grids.append(g)
+        hosts.append(A)
+        entries.append((g, T, None))
+    b = capi.Batch(entries, fp_mode="fma", mode="streams")
+    assert b.stats().grids == len(specs)
+    s = torch.cuda.current_stream()
+    b.run(s.cuda_stream)
+    capi.sync(s.cuda_stream)
+    for (name, n, T), g, A in zip(specs, grids, hosts):
+        ref = A.copy()
+        po.run(name, ref, n, T)
+        assert po.normwise_error(g.download(), ref, T) <= tol, (name, n, T)
+    b.close()
+
+
+def test_batch_work_item_schedules_refuse_3d_and_double():
+    g3 = DeviceGrid("j3d27pt", np.float32, [12, 12, 12])
+    for sched in ("persistent", "layered"):
+        with pytest.raises(capi.GbsError) as e:
+            capi.Batch([(g3, 2, None)], fp_mode="fma", mode=sched)
+        assert e.value.status == capi.GBS_ERR_UNSUPPORTED
+    g2 = DeviceGrid("star2d1r", np.float64, [40, 40])
+    with pytest.raises(capi.GbsError) as e:
+        capi.Batch([(g2, 2, None)], fp_mode="fma", mode="persistent")
+    assert e.value.status == capi.GBS_ERR_UNSUPPORTED

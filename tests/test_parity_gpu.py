@@ -195,3 +195,24 @@ def test_parity_3d_reference_init(name, dt):
     if has_exact(name):
         compare(name, A0, [n, n, n], T, dt, "exact", max_class(name, dt, "exact"))
     compare(name, A0, [n, n, n], T, dt, "fma", max_class(name, dt, "fma"))
+
+
+@pytest.mark.parametrize("name,dt", [("box3d1r", np.float64), ("star3d2r", np.float32), ("j3d27pt", np.float32)])
+def test_parity_3d_block_shapes(name, dt):
+    """Every built tile height gives the same bits (the arithmetic of a cell
+    does not depend on the tiling) and the oracle's result within tolerance."""
+    import ctypes
+    outs = []
+    for bs1 in (64, 32):
+        d, _ = capi.make_desc(name, dt, 70, 5, "fma", bt=1, bs1=bs1)
+        if capi.lib().gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) != capi.GBS_OK:
+            continue
+        A0, nn = random_grid(name, [70, 45, 150], dt, 400)
+        ref = A0.copy()
+        po.run(name, ref, nn, 5)
+        gpu = A0.copy()
+        d, _ = capi.make_desc(name, dt, nn, 5, fp_mode="fma", bt=1, bs1=bs1)
+        capi.run_host(d, gpu)
+        assert po.normwise_error(gpu, ref, 5) <= TOL[np.dtype(dt)]
+        outs.append(gpu)
+    assert len(outs) == 2 and np.array_equal(outs[0][1], outs[1][1])

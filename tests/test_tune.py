@@ -70,11 +70,16 @@ def test_shipped_table_is_consistent():
         line = line.split("#")[0].split()
         if not line:
             continue
-        name, dt, mode, cls, bt, sl, ms = line
+        if len(line) == 7:
+            name, dt, mode, cls, bt, sl, ms = line
+            bs1 = 0
+        else:
+            name, dt, mode, cls, bt, sl, bs1, ms = line
         s = capi.info(name)
-        assert 1 <= int(bt) <= 16 and int(sl) >= 0 and float(ms) > 0
-        d, _ = capi.make_desc(name, np.float32 if dt == "f32" else np.float64, 64, 1, mode)
-        assert capi.lib().gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_OK, s
+        assert 1 <= int(bt) <= 16 and int(sl) >= 0 and int(bs1) >= 0 and float(ms) > 0
+        d, _ = capi.make_desc(name, np.float32 if dt == "f32" else np.float64, 64, 1, mode, bt=int(bt),
+                              bs1=int(bs1))
+        assert capi.lib().gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_OK, (s, line)
 
 
 @pytest.mark.gpu
@@ -93,7 +98,7 @@ def test_tune_times_candidates(fresh_table, name, dtype, n):
     a.fill_uniform(1)
     b.fill_uniform(1)
     a.run(6, "fma")
-    b.run(6, "fma", bt=best["bt"], sl=best["sl"])
+    b.run(6, "fma", bt=best["bt"], sl=best["sl"], bs1=best["bs1"])
     torch.cuda.synchronize()
     capi.sync(0)
     assert torch.equal(a.plane(0), b.plane(0))
@@ -111,3 +116,39 @@ def test_model_prefers_fusion_when_memory_bound():
         assert 0 < ms.value < 1e3
         times.append(ms.value)
     assert times[0] > times[1] > times[2]
+
+
+def test_block_shape_choices():
+    """bs1 selects the 3-D tile height among the built shapes (gbs_plan
+    reports it); other heights, 2-D warps per CTA other than 4 and tile
+    widths other than one warp of 16-byte vectors are refused (host
+    arithmetic)."""
+    L = capi.lib()
+    heights = set()
+    for bs1 in (0, 64, 32):
+        d, _ = capi.make_desc("box3d1r", np.float64, 256, 10, "fma", bt=1, bs1=bs1)
+        pi = capi.PlanInfo()
+        assert L.gbs_plan(ctypes.byref(d), ctypes.byref(pi)) == capi.GBS_OK
+        assert bs1 == 0 or pi.bs1 == bs1
+        assert pi.bs2 == 64
+        heights.add(pi.bs1)
+    assert heights == {64, 32}
+    d, _ = capi.make_desc("box3d1r", np.float64, 256, 10, "fma", bt=1, bs1=48)
+    assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_ERR_UNSUPPORTED
+    d, _ = capi.make_desc("star2d1r", np.float32, 256, 10, "fma", bs1=8)
+    assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_ERR_UNSUPPORTED
+    d, _ = capi.make_desc("star2d1r", np.float32, 256, 10, "fma")
+    d.bs2 = 64
+    assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_ERR_UNSUPPORTED
+    d.bs2 = 128
+    assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_OK
+
+
+def test_table_records_block_shape(fresh_table):
+    d, _ = capi.make_desc("star3d2r", np.float32, 256, 0, "fma", bs1=32)
+    capi.check(capi.lib().gbs_tune_set(ctypes.byref(d), 1, 0, ctypes.c_double(0.5)))
+    d0, _ = capi.make_desc("star3d2r", np.float32, 256, 10, "fma")
+    assert capi.plan(d0).bs1 == 32          # bs1 = 0 resolves through the table
+    path = fresh_table / "t.txt"
+    tune.save(path)
+    assert "star3d2r f32 fma 24 1 0 32 0.5" in path.read_text()
