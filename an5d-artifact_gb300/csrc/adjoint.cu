@@ -270,21 +270,24 @@ __device__ __forceinline__ T row_value(const T *p, const T (&rows)[2 * R + 1][V]
 // at every halo cell h. One launch per step instead of the transposed engine
 // step, the halo kernel and the product kernel: 2-D grids are small enough
 // that a step is bound by kernel latency. The first `interior_blocks` CTAs
-// take (interior row, 32*V-column) units: each lane one aligned 16-byte
-// vector of V columns per row offset, the in-row neighbours from the
-// lanes up to R/V away (the warp's edge lanes load theirs); the CTAs after
-// them take the halo cells (one thread each).
+// take work units of one 32*V-column segment by `rows` interior rows: each
+// lane streams its aligned 16-byte vector of V columns down the rows,
+// keeping the 2R+1 rows of lam (and of u) that the current output row
+// needs in registers, so that every row is loaded once per unit; in-row
+// neighbours come from the lanes up to R/V away (the warp's edge lanes load
+// theirs). The CTAs after them take the halo cells (one thread each).
 template <class ST, typename T, bool WANT_COEF>
 __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constant__ AdjGeom g,
                                                             const T *__restrict__ lam, const T *__restrict__ u,
                                                             T *__restrict__ lam_out, T *__restrict__ hg,
                                                             double *__restrict__ part,
                                                             const __grid_constant__ LinCoef<T, ST::kTerms> cf,
-                                                            T inv_div, int interior_blocks) {
+                                                            T inv_div, int interior_blocks, int rows) {
   constexpr int NT = ST::kTerms;
   constexpr int NP = WANT_COEF ? NT : 1;
   constexpr int V = 16 / sizeof(T);
   constexpr int R = ST::kRad;
+  constexpr int W = 2 * R + 1;
   constexpr int SEG = 32 * V;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if ((int)blockIdx.x >= interior_blocks) {
@@ -299,53 +302,66 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
   for (int t = 0; t < NP; ++t) acc[t] = T(0);
   const int width = g.last - 2 * R;
   const int nseg = (width + SEG - 1) / SEG;
-  const long long units = (long long)(g.d0 - 2 * R) * nseg;
+  const int ni = g.d0 - 2 * R;
+  const int nblk = (ni + rows - 1) / rows;
+  const long long units = (long long)nblk * nseg;
   const long long nwarps = (long long)interior_blocks * (kAdjThreads / 32);
   for (long long un = (long long)blockIdx.x * (kAdjThreads / 32) + w; un < units; un += nwarps) {
-    const int ii = (int)(un / nseg), seg = (int)(un - (long long)ii * nseg);
-    const int i = R + ii;
+    const int blk = (int)(un / nseg), seg = (int)(un - (long long)blk * nseg);
+    const int ia = R + blk * rows, ib = min(ia + rows, g.d0 - R);  // output rows [ia, ib)
     const int c0 = R + seg * SEG + lane * V;        // the lane's first column; 16-byte aligned
     const int nvalid = min(V, g.last - R - c0);     // columns of the group inside the interior
-    const long long base = (long long)i * g.pitch + g.shift + c0;
-    // the 2R+1 row vectors of the unit, each loaded once
-    T lrow[2 * R + 1][V];
-    static_for<2 * R + 1>([&](auto DI) {
-      constexpr int d = decltype(DI)::value - R;
-      ld_vec<T, V>(lrow[d + R], lam + base + (long long)d * g.pitch);
+    const long long col = (long long)g.shift + c0;
+    // windows of rows i-R .. i+R (position d+R holds row i+d)
+    T lw[W][V], uw[W][V];
+    static_for<W - 1>([&](auto DI) {
+      constexpr int d = decltype(DI)::value - R;  // rows ia-R .. ia+R-1
+      ld_vec<T, V>(lw[d + R + 1], lam + (long long)(ia + d) * g.pitch + col);
+      if constexpr (WANT_COEF) ld_vec<T, V>(uw[d + R + 1], u + (long long)(ia + d) * g.pitch + col);
     });
-    T sv[V];
+#pragma unroll 1
+    for (int i = ia; i < ib; ++i) {
+      // slide: drop row i-R-1, load row i+R
+      static_for<W - 1>([&](auto DI) {
+        constexpr int d = decltype(DI)::value;
 #pragma unroll
-    for (int e = 0; e < V; ++e) sv[e] = T(0);
-    static_for<NT>([&](auto TI) {
-      constexpr int t = decltype(TI)::value;
-      constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-      static_for<V>([&](auto EI) {
-        constexpr int e = decltype(EI)::value;
-        sv[e] = fma(cf.c[t], row_value<V, R, -di, e - dj>(lam, lrow, base, g.pitch, lane), sv[e]);
+        for (int e = 0; e < V; ++e) {
+          lw[d][e] = lw[d + 1][e];
+          if constexpr (WANT_COEF) uw[d][e] = uw[d + 1][e];
+        }
       });
-    });
-    if constexpr (WANT_COEF) {
-      T urow[2 * R + 1][V];
-      static_for<2 * R + 1>([&](auto DI) {
-        constexpr int d = decltype(DI)::value - R;
-        ld_vec<T, V>(urow[d + R], u + base + (long long)d * g.pitch);
-      });
+      const long long base = (long long)i * g.pitch + col;
+      ld_vec<T, V>(lw[W - 1], lam + base + (long long)R * g.pitch);
+      if constexpr (WANT_COEF) ld_vec<T, V>(uw[W - 1], u + base + (long long)R * g.pitch);
+      T sv[V];
+#pragma unroll
+      for (int e = 0; e < V; ++e) sv[e] = T(0);
       static_for<NT>([&](auto TI) {
         constexpr int t = decltype(TI)::value;
         constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
         static_for<V>([&](auto EI) {
           constexpr int e = decltype(EI)::value;
-          const T uv = row_value<V, R, di, e + dj>(u, urow, base, g.pitch, lane);
-          if (e < nvalid) acc[t] = fma(lrow[R][e], uv, acc[t]);
+          sv[e] = fma(cf.c[t], row_value<V, R, -di, e - dj>(lam, lw, base, g.pitch, lane), sv[e]);
         });
       });
-    }
-    if (nvalid == V) {
-      st_vec<T, V>(lam_out + base, sv);
-    } else {
+      if constexpr (WANT_COEF) {
+        static_for<NT>([&](auto TI) {
+          constexpr int t = decltype(TI)::value;
+          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+          static_for<V>([&](auto EI) {
+            constexpr int e = decltype(EI)::value;
+            const T uv = row_value<V, R, di, e + dj>(u, uw, base, g.pitch, lane);
+            if (e < nvalid) acc[t] = fma(lw[R][e], uv, acc[t]);
+          });
+        });
+      }
+      if (nvalid == V) {
+        st_vec<T, V>(lam_out + base, sv);
+      } else {
 #pragma unroll
-      for (int e = 0; e < V; ++e)
-        if (e < nvalid) lam_out[base + e] = sv[e];
+        for (int e = 0; e < V; ++e)
+          if (e < nvalid) lam_out[base + e] = sv[e];
+      }
     }
   }
   if constexpr (WANT_COEF) {
@@ -676,14 +692,24 @@ cudaError_t run_fused2d(const AdjGeom &g, const void *lam, const void *u, void *
     const unsigned halo_blocks = (unsigned)((halo_threads + kAdjThreads - 1) / kAdjThreads);
     const int wave_c = wave_cached(adj2d_kernel<ST, T, true>);
     const int wave_n = wave_cached(adj2d_kernel<ST, T, false>);
+    // rows per work unit: about one unit per resident warp, at least 4 rows
+    // so that the 2R rows each unit loads to fill its window stay a minor cost
+    constexpr int SEG = 32 * (16 / sizeof(T));
+    const long long nseg = (g.last - 2 * ST::kRad + SEG - 1) / SEG;
+    const int ni = g.d0 - 2 * ST::kRad;
+    auto rows_for = [&](int wave) {
+      const long long warps = (long long)wave * (kAdjThreads / 32);
+      const long long per = (ni * nseg + warps - 1) / std::max(1LL, warps);
+      return (int)std::max<long long>(4, std::min<long long>(ni, per));
+    };
     if (want_coef)
       adj2d_kernel<ST, T, true><<<wave_c + halo_blocks, kAdjThreads, 0, s>>>(
           g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
-          part, cf, inv, wave_c);
+          part, cf, inv, wave_c, rows_for(wave_c));
     else
       adj2d_kernel<ST, T, false><<<wave_n + halo_blocks, kAdjThreads, 0, s>>>(
           g, static_cast<const T *>(lam), static_cast<const T *>(u), static_cast<T *>(lam_out), static_cast<T *>(hg),
-          part, cf, inv, wave_n);
+          part, cf, inv, wave_n, rows_for(wave_n));
     return cudaGetLastError();
   }
 }
@@ -1117,6 +1143,20 @@ gbs_status gbs_adjoint_backward_slots(const gbs_desc *d, const void *dev_lamT, v
     }
     cudaEventRecord(setup, s);
     cudaStreamWaitEvent(s2, setup, 0);
+    // recompute degree: 2-D grids use the forward's fused degree, each
+    // launch also storing its intermediate states (stash mode); 3-D one step
+    // per launch
+    int bre = 1;
+    if (g.dim == 2) {
+      gbs_desc dp = *d;
+      dp.timestep = std::max(1, w.C);
+      gbs_plan_info pi{};
+      if ((st = gbs_plan(&dp, &pi)) != GBS_OK) {
+        release();
+        return st;
+      }
+      bre = std::max(1, pi.bt);
+    }
     // recompute u_{t0} .. u_{t0+c-1} of chunk j into buffer j % 2 on s2
     auto recompute = [&](int j) -> gbs_status {
       const int b = j & 1;
@@ -1126,10 +1166,14 @@ gbs_status gbs_adjoint_backward_slots(const gbs_desc *d, const void *dev_lamT, v
       cudaError_t ce = cudaMemcpyAsync(buf, ws + w.off_cp + (size_t)j * w.plane_bytes, w.plane_bytes,
                                        cudaMemcpyDeviceToDevice, s2);
       if (ce != cudaSuccess) return cuda_fail(ce, "adjoint: restore");
-      for (int k = 1; k < c; ++k) {
-        gbs_status r = launch_block(d, L, coef.data(), div, eps, 0, 1, buf + (size_t)(k - 1) * w.plane_bytes,
-                                    buf + (size_t)k * w.plane_bytes, s2, err);
+      for (int k = 1; k < c;) {
+        // one launch of bb steps from slot k-1: slots k .. k+bb-1
+        const int bb = std::min(bre, c - k);
+        gbs_status r = launch_block_stash(d, L, coef.data(), div, eps, 0, bb, buf + (size_t)(k - 1) * w.plane_bytes,
+                                          buf + (size_t)(k - 1 + bb) * w.plane_bytes,
+                                          bb > 1 ? buf + (size_t)k * w.plane_bytes : nullptr, s2, err);
         if (r != GBS_OK) return r;
+        k += bb;
       }
       cudaEventRecord(ready[b], s2);
       return GBS_OK;

@@ -115,6 +115,8 @@ __device__ __noinline__ bool run_item(const GridDev &g, const Item &it, float *r
     p.rdiv = g.rdiv;
     p.eps = g.eps;
     p.divmode = g.divmode;
+    p.stash = nullptr;
+    p.stash_stride = 0;
   }
   __syncwarp();
   bool ok;

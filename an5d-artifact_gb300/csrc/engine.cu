@@ -475,7 +475,13 @@ gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_
 // writes them, divisor and eps resolved, sl 0 = one wave.
 gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, double div, double eps, int sl,
                         int b, const void *src, void *dst, cudaStream_t stream, int *err) {
+  return launch_block_stash(d, L, coef, div, eps, sl, b, src, dst, nullptr, stream, err);
+}
+
+gbs_status launch_block_stash(const gbs_desc *d, const Layout &L, const double *coef, double div, double eps, int sl,
+                              int b, const void *src, void *dst, void *stash, cudaStream_t stream, int *err) {
   const gbs_stencil_def_t *s = stencil_def(d->stencil);
+  if (stash && s->dim != 2) return fail(GBS_ERR_UNSUPPORTED, "stashed launches take 2-D grids");
   const int fma = d->fp_mode == GBS_FP_FMA ? 1 : 0;
   const Picks &pk = picks(d->stencil, d->dtype, fma);
   if (b < 1 || b > pk.maxb)
@@ -502,6 +508,8 @@ gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, 
       a.div = div;
       a.eps = eps;
       a.div_proven = d->dtype == GBS_F32 && div_proven_exact(div);
+      a.stash = stash;
+      a.stash_stride = L.plane;
       if (!pk.l2[b]) return fail(GBS_ERR_UNSUPPORTED, "no 2-D kernel for b=%d", b);
       cudaError_t e = pk.l2[b](a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");

@@ -59,6 +59,11 @@ gbs_status error_word(int **out);
 gbs_status run_loop(const gbs_desc *d, const Layout &L, void *dev_A, cudaStream_t stream, int *err);
 gbs_status launch_block(const gbs_desc *d, const Layout &L, const double *coef, double div, double eps, int sl,
                         int b, const void *src, void *dst, cudaStream_t stream, int *err);
+// launch_block that also stores the states after 1 .. b-1 steps (interior
+// cells) to the planes stash, stash + plane, ... (2-D grids only; stash may
+// be null)
+gbs_status launch_block_stash(const gbs_desc *d, const Layout &L, const double *coef, double div, double eps, int sl,
+                              int b, const void *src, void *dst, void *stash, cudaStream_t stream, int *err);
 int max_bt(int sid, int dtype, int fma);
 // the tuning table's (bt, sl) for d's stencil, dtype, mode and size class
 bool tuned_lookup(const gbs_desc *d, int *bt, int *sl, int *bs1 = nullptr);

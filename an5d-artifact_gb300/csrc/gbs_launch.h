@@ -15,6 +15,9 @@ struct Launch2D {
   const double *coef;
   double div, eps;
   bool div_proven;    // the one-correction quotient is exact for every float input
+  void *stash;        // not null: level l < b also stores its interior cells to
+                      // stash + (l-1)*stash_stride elements (the states between)
+  long long stash_stride;
 };
 
 // One launch of the 3-D family (see kernel3d.cuh).

@@ -54,6 +54,8 @@ template <typename T, int NT> struct Params2D {
   T coef[NT];
   T div, rdiv, eps;    // divisor, RN(1/divisor), gradient epsilon
   int divmode;         // 0: no division (folded into coef), 1: checked, 2: proven fast path
+  T *stash;            // not null: level l < b also stores its interior cells to stash + (l-1)*stash_stride
+  long long stash_stride;
 };
 
 // y / div as the params ask (see div_by / div_by_fast)
@@ -330,6 +332,21 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
     static_for<B>([&](auto LI) {
       constexpr int l = decltype(LI)::value;
       level2d<ST, T, FMA, UNR, careful, ph, V, NSTAGE>(win[l], x, pp - (l + 1) * R, edge, col0, carry, p);
+      if constexpr (l + 1 < B) {
+        // stash mode: this level's row, the state after l+1 steps, in the
+        // item's output rows and columns (valid at every level)
+        const int ql = pp - (l + 1) * R;
+        if (p.stash && ql >= i0 && ql < i1) {
+          T *d = p.stash + (long long)l * p.stash_stride + ws + lane * V + (long long)ql * pitch;
+          if (store_all) {
+            st_vec_global<T, V>(d, x);
+          } else {
+#pragma unroll
+            for (int e = 0; e < V; ++e)
+              if (col0 + e >= cs && col0 + e < ce) st_global(d + e, x[e]);
+          }
+        }
+      }
     });
     const int q = pp - B * R;
     if (q >= i0 && q < i1) {
@@ -463,6 +480,8 @@ cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
   p.div = (T)a.div;
   p.rdiv = div_reciprocal<T>(a.div);
   p.eps = (T)a.eps;
+  p.stash = static_cast<T *>(a.stash);
+  p.stash_stride = a.stash_stride;
   const size_t smem = (size_t)WPC * NSTAGE * (32 * V * sizeof(T) + sizeof(uint64_t));
   const long long warps = (long long)a.nstrips * a.nblocks;
   const long long grid = (warps + WPC - 1) / WPC;

@@ -81,6 +81,7 @@ def main():
     ap.add_argument("--stencils", default="", help="comma-separated subset")
     ap.add_argument("--dtypes", default="float32,float64")
     ap.add_argument("--modes", default="fma,exact")
+    ap.add_argument("--sizes", default="", help="comma-separated interior sides (default: the table's sizes)")
     ap.add_argument("--log", default="", help="also write every candidate's timing (JSON lines)")
     ap.add_argument("--fresh", action="store_true",
                     help="start from an empty table (default: re-tune into the shipped one)")
@@ -95,10 +96,12 @@ def main():
         s = capi.info(name)
         for dt in args.dtypes.split(","):
             for mode in args.modes.split(","):
-                for n in TABLE_SIZES[s["dim"]]:
+                sizes = [int(x) for x in args.sizes.split(",")] if args.sizes else TABLE_SIZES[s["dim"]]
+                for n in sizes:
                     best, cands = tune(name, np.dtype(dt), n, mode)
                     print(f"{name:11s} {dt:8s} {mode:5s} n={n:6d} bt={best['bt']} sl={best['sl']} "
-                          f"{best['ms_per_step']:.4f} ms/step ({len(cands)} candidates)", flush=True)
+                          f"bs1={best['bs1']} {best['ms_per_step']:.4f} ms/step ({len(cands)} candidates)",
+                          flush=True)
                     if log:
                         log.write(json.dumps({"stencil": name, "dtype": dt, "mode": mode, "n": n,
                                               "candidates": cands}) + "\n")
