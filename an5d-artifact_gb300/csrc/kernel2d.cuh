@@ -168,14 +168,22 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
           constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
           static_assert(di == 0 || dj == 0, "direct 2-D form expects off-centre rows at dj == 0");
           constexpr int slot = wslot<UNR, W>(PH, R + di);
-          static_for<V>([&](auto EI) {
-            constexpr int e = decltype(EI)::value;
-            T a;
-            if constexpr (dj == 0) a = win[slot][e];
-            else a = ext[R + e + dj];
-            if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
-            else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
-          });
+          if constexpr (FMA) {
+            fma_vec<T, t == 0, true>(y, p.coef[t], [&](auto EI) -> T {
+              constexpr int e = decltype(EI)::value;
+              if constexpr (dj == 0) return win[slot][e];
+              else return ext[R + e + dj];
+            });
+          } else {
+            static_for<V>([&](auto EI) {
+              constexpr int e = decltype(EI)::value;
+              T a;
+              if constexpr (dj == 0) a = win[slot][e];
+              else a = ext[R + e + dj];
+              if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
+              else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
+            });
+          }
         });
         if constexpr (ST::kHasDiv && !FMA) {  // FMA mode: folded into the coefficients
 #pragma unroll
@@ -204,12 +212,17 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
       constexpr int t = decltype(TI)::value;
       constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
       constexpr int slot = wslot<UNR, W>(PH, R - di);
-      static_for<V>([&](auto EI) {
-        constexpr int e = decltype(EI)::value;
-        const T a = ext[R + e + dj];
-        if constexpr (t == 0) win[slot][e] = A::mul(p.coef[t], a);
-        else win[slot][e] = term_next<T, FMA>(win[slot][e], p.coef[t], a);
-      });
+      if constexpr (FMA) {
+        fma_vec<T, t == 0, false>(win[slot], p.coef[t],
+                                  [&](auto EI) -> T { return ext[R + decltype(EI)::value + dj]; });
+      } else {
+        static_for<V>([&](auto EI) {
+          constexpr int e = decltype(EI)::value;
+          const T a = ext[R + e + dj];
+          if constexpr (t == 0) win[slot][e] = A::mul(p.coef[t], a);
+          else win[slot][e] = term_next<T, FMA>(win[slot][e], p.coef[t], a);
+        });
+      }
     });
     constexpr int oslot = wslot<UNR, W>(PH, 0);
 #pragma unroll
