@@ -98,8 +98,9 @@ gbs_status check_desc(const gbs_desc *d) {
   if (d->bt < 0 || d->sl < 0 || d->bs1 < 0 || d->bs2 < 0)
     return fail(GBS_ERR_INVALID, "bt/bs1/bs2/sl must be >= 0");
   const int V = d->dtype == GBS_F64 ? 2 : 4;
-  if (d->bs2 != 0 && d->bs2 != 32 * V)
-    return fail(GBS_ERR_UNSUPPORTED, "bs2 (tile columns) must be 0 or %d for this element type", 32 * V);
+  if (d->bs2 != 0 && d->bs2 != 32 * V && !(s->dim == 2 && d->bs2 == 64 * V))
+    return fail(GBS_ERR_UNSUPPORTED, "bs2 (tile columns) must be 0, %d%s", 32 * V,
+                s->dim == 2 ? " or twice that" : "");
   if (s->dim == 2 && d->bs1 != 0 && d->bs1 != kWarpsPerCta2D)
     return fail(GBS_ERR_UNSUPPORTED, "bs1 (warps per CTA) of a 2-D grid must be 0 or %d", kWarpsPerCta2D);
   return GBS_OK;
@@ -118,9 +119,10 @@ Layout make_layout(const gbs_desc *d) {
   const int inner = L.dims[s->dim - 1];
   // column c at element shift + c; the first interior column is 16-byte aligned
   L.shift = (L.V - s->rad % L.V) % L.V;
-  // every 32*V-element window starting at an aligned element < shift + inner
-  // must fit in the row
-  const long long need = (long long)L.shift + inner + 32 * L.V;
+  // every window a kernel streams (32 lanes of one 16-byte vector each, or of
+  // two in 2-D) starting at an aligned element < shift + inner must fit in
+  // the row
+  const long long need = (long long)L.shift + inner + (s->dim == 2 ? 64 : 32) * L.V;
   const long long align = 128 / (long long)L.esize;
   L.pitch = (need + align - 1) / align * align;
   L.rows = s->dim == 2 ? (long long)L.dims[0] : (long long)L.dims[0] * L.dims[1];
@@ -240,11 +242,19 @@ long long resident_warps_2d(int sid, int dtype, int fma, int b) {
   return (long long)c * sm_count();
 }
 
-Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident) {
+int lane_elems_2d(int sid, int dtype, int fma, int b) {
+  const Picks &pk = picks(sid, dtype, fma);
+  return (b >= 1 && b <= kMaxB && pk.l2[b]) ? pk.lv2[b] : 0;
+}
+
+Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident, int lv) {
   Geometry2D g{};
   const int R = L.rad, V = L.V;
   g.b = b;
-  g.wout = ((32 * V - 2 * b * R - (V - 1)) / V) * V;
+  g.lv = lv > 0 ? lv : V;
+  // window starts are 16-byte aligned, so the strip can start up to V-1
+  // columns inside it
+  g.wout = ((32 * g.lv - 2 * b * R - (V - 1)) / V) * V;
   const int ni = L.dims[0] - 2 * R, nj = L.dims[1] - 2 * R;
   g.nstrips = g.wout > 0 ? (nj + g.wout - 1) / g.wout : 1;
   int sl = sl_req;
@@ -369,7 +379,7 @@ gbs_status validate3d(const Layout &L, const Geometry3D &g) {
 
 // Every address range a 2-D launch touches, checked against the buffer.
 gbs_status validate2d(const Layout &L, const Geometry2D &g) {
-  const int R = L.rad, V = L.V, ROW = 32 * V;
+  const int R = L.rad, V = L.V, ROW = 32 * (g.lv > 0 ? g.lv : V);
   if (g.wout <= 0) return fail(GBS_ERR_UNSUPPORTED, "fused degree %d leaves no output columns", g.b);
   if (L.shift % 1 != 0 || (L.pitch * (long long)L.esize) % 16 != 0)
     return fail(GBS_ERR_INVALID, "internal: row pitch not 16-byte aligned");
@@ -397,10 +407,35 @@ using namespace gbs;
 // device state: error word, cached buffer, stream
 // ---------------------------------------------------------------------------
 namespace {
+// Dense rows <-> the engine layout's padded rows, on the device: row r of
+// `rows` rows of `words` 32-bit words. A host copy of a dense grid into a
+// dense device buffer is one contiguous transfer (full link speed); the
+// strided layout change then runs at HBM speed instead of as one copy
+// descriptor per row.
+__global__ void repitch_kernel(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, long long rows,
+                               int words, long long src_stride, long long dst_stride) {
+  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    const uint32_t *a = src + r * src_stride;
+    uint32_t *b = dst + r * dst_stride;
+    for (int c = threadIdx.x; c < words; c += blockDim.x) b[c] = a[c];
+  }
+}
+
+cudaError_t repitch(const void *src, void *dst, long long rows, size_t row_bytes, size_t src_pitch_bytes,
+                    size_t dst_pitch_bytes, cudaStream_t s) {
+  const long long blocks = std::min<long long>(rows, 152LL * 16);
+  repitch_kernel<<<(unsigned)std::max<long long>(1, blocks), 256, 0, s>>>(
+      static_cast<const uint32_t *>(src), static_cast<uint32_t *>(dst), rows, (int)(row_bytes / 4),
+      (long long)(src_pitch_bytes / 4), (long long)(dst_pitch_bytes / 4));
+  return cudaGetLastError();
+}
+
 struct DeviceState {
   int *err = nullptr;          // error word of the kernels (device)
   void *buf = nullptr;         // gbs_run's cached grid buffer
   size_t buf_bytes = 0;
+  void *dense = nullptr;       // gbs_run's cached staging buffer (the host grid's dense layout)
+  size_t dense_bytes = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -488,7 +523,11 @@ gbs_status launch_block_stash(const gbs_desc *d, const Layout &L, const double *
     return fail(GBS_ERR_UNSUPPORTED, "no kernel of degree %d built for %s", b, s->name);
   {
     if (s->dim == 2) {
-      Geometry2D g = geometry2d(L, b, sl, resident_warps_2d(d->stencil, d->dtype, fma, b));
+      Geometry2D g = geometry2d(L, b, sl, resident_warps_2d(d->stencil, d->dtype, fma, b),
+                                lane_elems_2d(d->stencil, d->dtype, fma, b));
+      if (d->bs2 != 0 && d->bs2 != 32 * g.lv)
+        return fail(GBS_ERR_UNSUPPORTED, "bs2=%d: the 2-D kernel of degree %d has %d-column windows", d->bs2, b,
+                    32 * g.lv);
       gbs_status st = validate2d(L, g);
       if (st != GBS_OK) return st;
       Launch2D a{};
@@ -611,15 +650,19 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
   out->bt = bt;
   out->launches = (int)split_steps(d->timestep, bt).size();
   if (s->dim == 2) {
-    Geometry2D g = geometry2d(L, bt, sl, resident_warps_2d(d->stencil, d->dtype, fma, bt));
+    Geometry2D g = geometry2d(L, bt, sl, resident_warps_2d(d->stencil, d->dtype, fma, bt),
+                              lane_elems_2d(d->stencil, d->dtype, fma, bt));
+    if (d->bs2 != 0 && d->bs2 != 32 * g.lv)
+      return fail(GBS_ERR_UNSUPPORTED, "bs2=%d: the 2-D kernel of degree %d has %d-column windows", d->bs2, bt,
+                  32 * g.lv);
     st = validate2d(L, g);
     if (st != GBS_OK) return st;
     out->bs1 = kWarpsPerCta2D;
-    out->bs2 = 32 * L.V;
+    out->bs2 = 32 * g.lv;
     out->sl = g.sl;
     out->ctas = (g.nstrips * g.nblocks + 3) / 4;
     out->valid_w = g.wout;
-    const double cols = 32.0 * L.V, rows = g.sl + 2.0 * bt * L.rad;
+    const double cols = 32.0 * g.lv, rows = g.sl + 2.0 * bt * L.rad;
     out->redundancy = (cols * rows) / ((double)g.wout * g.sl);
   } else {
     const int v = variant_3d(d, bt);
@@ -719,7 +762,23 @@ gbs_status gbs_run(const gbs_desc *d, void *host_A, double *ms_out) {
     // margins are never part of a result but are read by edge windows
     if ((e = cudaMemset(s->buf, 0, L.bytes)) != cudaSuccess) return cuda_fail(e, "cudaMemset(grid)");
   }
-  if ((st = gbs_upload(d, host_A, s->buf, s->stream)) != GBS_OK) return st;
+  // host grid -> dense staging buffer (one contiguous copy) -> engine layout
+  const size_t row_bytes = (size_t)L.dims[L.dim - 1] * L.esize;
+  const long long nrows = 2 * (long long)L.rows;
+  const size_t dense_bytes = row_bytes * (size_t)nrows;
+  if (s->dense_bytes < dense_bytes) {
+    if (s->dense) cudaFree(s->dense);
+    s->dense = nullptr;
+    s->dense_bytes = 0;
+    if ((e = cudaMalloc(&s->dense, dense_bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(staging)");
+    s->dense_bytes = dense_bytes;
+  }
+  char *padded = static_cast<char *>(s->buf) + L.shift * L.esize;
+  const size_t pitch_bytes = (size_t)L.pitch * L.esize;
+  if ((e = cudaMemcpyAsync(s->dense, host_A, dense_bytes, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+    return cuda_fail(e, "upload");
+  if ((e = repitch(s->dense, padded, nrows, row_bytes, row_bytes, pitch_bytes, s->stream)) != cudaSuccess)
+    return cuda_fail(e, "upload (layout)");
   if ((e = cudaEventRecord(s->ev0, s->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
   st = run_loop(d, L, s->buf, s->stream, s->err);
   if (st != GBS_OK) {
@@ -727,7 +786,10 @@ gbs_status gbs_run(const gbs_desc *d, void *host_A, double *ms_out) {
     return st;
   }
   if ((e = cudaEventRecord(s->ev1, s->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
-  if ((st = gbs_download(d, s->buf, host_A, s->stream)) != GBS_OK) return st;
+  if ((e = repitch(padded, s->dense, nrows, row_bytes, pitch_bytes, row_bytes, s->stream)) != cudaSuccess)
+    return cuda_fail(e, "download (layout)");
+  if ((e = cudaMemcpyAsync(host_A, s->dense, dense_bytes, cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
+    return cuda_fail(e, "download");
   {
     // gbs_sync takes the lock through error_word(); read the word directly
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
@@ -751,8 +813,11 @@ void gbs_release_cache(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto &s : g_dev) {
     if (s.buf) cudaFree(s.buf);
+    if (s.dense) cudaFree(s.dense);
     s.buf = nullptr;
     s.buf_bytes = 0;
+    s.dense = nullptr;
+    s.dense_bytes = 0;
   }
 }
 

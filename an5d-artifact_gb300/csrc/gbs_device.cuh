@@ -143,9 +143,15 @@ __device__ __forceinline__ void st_vec(T *p, const T (&x)[V]) {
 // it cannot alias shared memory.
 template <typename T, int V>
 __device__ __forceinline__ void st_vec_global(T *p, const T (&x)[V]) {
-  static_assert(sizeof(T) * V == 16, "16-byte vectors only");
-  if constexpr (std::is_same<T, float>::value) __stcg(reinterpret_cast<float4 *>(p), make_float4(x[0], x[1], x[2], x[3]));
-  else __stcg(reinterpret_cast<double2 *>(p), make_double2(x[0], x[1]));
+  static_assert(sizeof(T) * V % 16 == 0, "whole 16-byte vectors only");
+  constexpr int VV = 16 / sizeof(T);
+#pragma unroll
+  for (int k = 0; k < V / VV; ++k) {
+    if constexpr (std::is_same<T, float>::value)
+      __stcg(reinterpret_cast<float4 *>(p) + k, make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]));
+    else
+      __stcg(reinterpret_cast<double2 *>(p) + k, make_double2(x[2 * k], x[2 * k + 1]));
+  }
 }
 template <typename T>
 __device__ __forceinline__ void st_global(T *p, T v) { __stcg(p, v); }

@@ -54,6 +54,7 @@ struct Picks {
   int maxb;
   Launch2DFn l2[kMaxB + 1];
   Occupancy2DFn o2[kMaxB + 1];
+  int lv2[kMaxB + 1];           // elements per lane of the 2-D launcher (its window is 32 lanes wide)
   Launch3DFn l3[kMaxB + 1][kVar3];
   Occupancy3DFn o3[kMaxB + 1][kVar3];
   int tj3[kMaxB + 1][kVar3];    // tile rows of the 3-D launcher (0: variant not built)

@@ -116,7 +116,9 @@ gbs_status gbs_stencil_info(int id, int *dim, int *rad, int *nterms, int *fpp);
  * both planes are copied to the device, advanced d->timestep steps and copied
  * back. *ms_out (may be NULL) receives the device time of the time loop only,
  * excluding allocation and copies, as the reference's return value does
- * (_host.cu:39-40,559-560). The device buffer is cached between calls. */
+ * (_host.cu:39-40,559-560). The device buffers (the grid in the engine layout
+ * and a dense staging copy, through which the host copies run as single
+ * contiguous transfers) are cached between calls. */
 gbs_status gbs_run(const gbs_desc *d, void *host_A, double *ms_out);
 
 /* Same time loop on a device buffer in the engine's layout (gbs_get_layout),
