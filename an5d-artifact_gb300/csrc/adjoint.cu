@@ -1143,11 +1143,11 @@ gbs_status gbs_adjoint_backward_slots(const gbs_desc *d, const void *dev_lamT, v
     }
     cudaEventRecord(setup, s);
     cudaStreamWaitEvent(s2, setup, 0);
-    // recompute degree: 2-D grids use the forward's fused degree, each
-    // launch also storing its intermediate states (stash mode); 3-D one step
-    // per launch
+    // recompute degree: 2-D grids in FMA mode use the forward's fused degree
+    // (at most the largest stash-mode degree), each launch also storing its
+    // intermediate states; otherwise one step per launch
     int bre = 1;
-    if (g.dim == 2) {
+    if (g.dim == 2 && d->fp_mode == GBS_FP_FMA) {
       gbs_desc dp = *d;
       dp.timestep = std::max(1, w.C);
       gbs_plan_info pi{};
@@ -1155,7 +1155,7 @@ gbs_status gbs_adjoint_backward_slots(const gbs_desc *d, const void *dev_lamT, v
         release();
         return st;
       }
-      bre = std::max(1, pi.bt);
+      bre = std::max(1, std::min(pi.bt, kMaxStashB));
     }
     // recompute u_{t0} .. u_{t0+c-1} of chunk j into buffer j % 2 on s2
     auto recompute = [&](int j) -> gbs_status {

@@ -98,9 +98,8 @@ gbs_status check_desc(const gbs_desc *d) {
   if (d->bt < 0 || d->sl < 0 || d->bs1 < 0 || d->bs2 < 0)
     return fail(GBS_ERR_INVALID, "bt/bs1/bs2/sl must be >= 0");
   const int V = d->dtype == GBS_F64 ? 2 : 4;
-  if (d->bs2 != 0 && d->bs2 != 32 * V && !(s->dim == 2 && d->bs2 == 64 * V))
-    return fail(GBS_ERR_UNSUPPORTED, "bs2 (tile columns) must be 0, %d%s", 32 * V,
-                s->dim == 2 ? " or twice that" : "");
+  if (d->bs2 != 0 && d->bs2 != 32 * V)
+    return fail(GBS_ERR_UNSUPPORTED, "bs2 (tile columns) must be 0 or %d for this element type", 32 * V);
   if (s->dim == 2 && d->bs1 != 0 && d->bs1 != kWarpsPerCta2D)
     return fail(GBS_ERR_UNSUPPORTED, "bs1 (warps per CTA) of a 2-D grid must be 0 or %d", kWarpsPerCta2D);
   return GBS_OK;
@@ -119,10 +118,9 @@ Layout make_layout(const gbs_desc *d) {
   const int inner = L.dims[s->dim - 1];
   // column c at element shift + c; the first interior column is 16-byte aligned
   L.shift = (L.V - s->rad % L.V) % L.V;
-  // every window a kernel streams (32 lanes of one 16-byte vector each, or of
-  // two in 2-D) starting at an aligned element < shift + inner must fit in
-  // the row
-  const long long need = (long long)L.shift + inner + (s->dim == 2 ? 64 : 32) * L.V;
+  // every 32*V-element window starting at an aligned element < shift + inner
+  // must fit in the row
+  const long long need = (long long)L.shift + inner + 32 * L.V;
   const long long align = 128 / (long long)L.esize;
   L.pitch = (need + align - 1) / align * align;
   L.rows = s->dim == 2 ? (long long)L.dims[0] : (long long)L.dims[0] * L.dims[1];
@@ -242,19 +240,13 @@ long long resident_warps_2d(int sid, int dtype, int fma, int b) {
   return (long long)c * sm_count();
 }
 
-int lane_elems_2d(int sid, int dtype, int fma, int b) {
-  const Picks &pk = picks(sid, dtype, fma);
-  return (b >= 1 && b <= kMaxB && pk.l2[b]) ? pk.lv2[b] : 0;
-}
-
-Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident, int lv) {
+Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident) {
   Geometry2D g{};
   const int R = L.rad, V = L.V;
   g.b = b;
-  g.lv = lv > 0 ? lv : V;
   // window starts are 16-byte aligned, so the strip can start up to V-1
   // columns inside it
-  g.wout = ((32 * g.lv - 2 * b * R - (V - 1)) / V) * V;
+  g.wout = ((32 * V - 2 * b * R - (V - 1)) / V) * V;
   const int ni = L.dims[0] - 2 * R, nj = L.dims[1] - 2 * R;
   g.nstrips = g.wout > 0 ? (nj + g.wout - 1) / g.wout : 1;
   int sl = sl_req;
@@ -379,7 +371,7 @@ gbs_status validate3d(const Layout &L, const Geometry3D &g) {
 
 // Every address range a 2-D launch touches, checked against the buffer.
 gbs_status validate2d(const Layout &L, const Geometry2D &g) {
-  const int R = L.rad, V = L.V, ROW = 32 * (g.lv > 0 ? g.lv : V);
+  const int R = L.rad, V = L.V, ROW = 32 * V;
   if (g.wout <= 0) return fail(GBS_ERR_UNSUPPORTED, "fused degree %d leaves no output columns", g.b);
   if (L.shift % 1 != 0 || (L.pitch * (long long)L.esize) % 16 != 0)
     return fail(GBS_ERR_INVALID, "internal: row pitch not 16-byte aligned");
@@ -523,11 +515,7 @@ gbs_status launch_block_stash(const gbs_desc *d, const Layout &L, const double *
     return fail(GBS_ERR_UNSUPPORTED, "no kernel of degree %d built for %s", b, s->name);
   {
     if (s->dim == 2) {
-      Geometry2D g = geometry2d(L, b, sl, resident_warps_2d(d->stencil, d->dtype, fma, b),
-                                lane_elems_2d(d->stencil, d->dtype, fma, b));
-      if (d->bs2 != 0 && d->bs2 != 32 * g.lv)
-        return fail(GBS_ERR_UNSUPPORTED, "bs2=%d: the 2-D kernel of degree %d has %d-column windows", d->bs2, b,
-                    32 * g.lv);
+      Geometry2D g = geometry2d(L, b, sl, resident_warps_2d(d->stencil, d->dtype, fma, b));
       gbs_status st = validate2d(L, g);
       if (st != GBS_OK) return st;
       Launch2D a{};
@@ -549,8 +537,9 @@ gbs_status launch_block_stash(const gbs_desc *d, const Layout &L, const double *
       a.div_proven = d->dtype == GBS_F32 && div_proven_exact(div);
       a.stash = stash;
       a.stash_stride = L.plane;
-      if (!pk.l2[b]) return fail(GBS_ERR_UNSUPPORTED, "no 2-D kernel for b=%d", b);
-      cudaError_t e = pk.l2[b](a, stream);
+      Launch2DFn fn = stash ? pk.l2s[b] : pk.l2[b];
+      if (!fn) return fail(GBS_ERR_UNSUPPORTED, "no 2-D kernel%s for b=%d", stash ? " in stash mode" : "", b);
+      cudaError_t e = fn(a, stream);
       if (e != cudaSuccess) return cuda_fail(e, "2-D stencil launch");
     } else {
       const int v = variant_3d(d, b);
@@ -650,19 +639,15 @@ gbs_status gbs_plan(const gbs_desc *d, gbs_plan_info *out) {
   out->bt = bt;
   out->launches = (int)split_steps(d->timestep, bt).size();
   if (s->dim == 2) {
-    Geometry2D g = geometry2d(L, bt, sl, resident_warps_2d(d->stencil, d->dtype, fma, bt),
-                              lane_elems_2d(d->stencil, d->dtype, fma, bt));
-    if (d->bs2 != 0 && d->bs2 != 32 * g.lv)
-      return fail(GBS_ERR_UNSUPPORTED, "bs2=%d: the 2-D kernel of degree %d has %d-column windows", d->bs2, bt,
-                  32 * g.lv);
+    Geometry2D g = geometry2d(L, bt, sl, resident_warps_2d(d->stencil, d->dtype, fma, bt));
     st = validate2d(L, g);
     if (st != GBS_OK) return st;
     out->bs1 = kWarpsPerCta2D;
-    out->bs2 = 32 * g.lv;
+    out->bs2 = 32 * L.V;
     out->sl = g.sl;
     out->ctas = (g.nstrips * g.nblocks + 3) / 4;
     out->valid_w = g.wout;
-    const double cols = 32.0 * g.lv, rows = g.sl + 2.0 * bt * L.rad;
+    const double cols = 32.0 * L.V, rows = g.sl + 2.0 * bt * L.rad;
     out->redundancy = (cols * rows) / ((double)g.wout * g.sl);
   } else {
     const int v = variant_3d(d, bt);

@@ -25,7 +25,6 @@ struct Layout {
 
 struct Geometry2D {
   int b, wout, nstrips, nblocks, sl;
-  int lv;  // elements per lane: the warp's window is 32 * lv columns
 };
 
 struct Geometry3D {
@@ -53,9 +52,7 @@ gbs_status check_desc(const gbs_desc *d);
 Layout make_layout(const gbs_desc *d);
 std::vector<int> split_steps(int T, int bt);
 // resident_warps: warps the GPU holds at once for this kernel (0 = unknown)
-Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident_warps, int lv = 0);
-// elements per lane of the 2-D launcher of degree b (0: none built)
-int lane_elems_2d(int sid, int dtype, int fma, int b);
+Geometry2D geometry2d(const Layout &L, int b, int sl_req, long long resident_warps);
 long long resident_warps_2d(int sid, int dtype, int fma, int b);
 gbs_status validate2d(const Layout &L, const Geometry2D &g);
 gbs_status error_word(int **out);

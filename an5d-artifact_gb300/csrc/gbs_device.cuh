@@ -143,15 +143,9 @@ __device__ __forceinline__ void st_vec(T *p, const T (&x)[V]) {
 // it cannot alias shared memory.
 template <typename T, int V>
 __device__ __forceinline__ void st_vec_global(T *p, const T (&x)[V]) {
-  static_assert(sizeof(T) * V % 16 == 0, "whole 16-byte vectors only");
-  constexpr int VV = 16 / sizeof(T);
-#pragma unroll
-  for (int k = 0; k < V / VV; ++k) {
-    if constexpr (std::is_same<T, float>::value)
-      __stcg(reinterpret_cast<float4 *>(p) + k, make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]));
-    else
-      __stcg(reinterpret_cast<double2 *>(p) + k, make_double2(x[2 * k], x[2 * k + 1]));
-  }
+  static_assert(sizeof(T) * V == 16, "16-byte vectors only");
+  if constexpr (std::is_same<T, float>::value) __stcg(reinterpret_cast<float4 *>(p), make_float4(x[0], x[1], x[2], x[3]));
+  else __stcg(reinterpret_cast<double2 *>(p), make_double2(x[0], x[1]));
 }
 template <typename T>
 __device__ __forceinline__ void st_global(T *p, T v) { __stcg(p, v); }
@@ -220,35 +214,6 @@ __device__ __forceinline__ T term_next(T acc, T c, T a) {
   using A = Arith<T>;
   if constexpr (FMA) return A::fma(c, a, acc);
   else return A::add(acc, A::mul(c, a));
-}
-
-// acc[e] = c * a(e) (FIRST) or c * a(e) + acc[e], for e < V, in FMA mode: a(e)
-// takes IC<e>. With PAIR, float pairs go through the paired FP32
-// instructions of sm_100 and later (__fmul2_rn / __ffma2_rn), which round
-// each component as __fmul_rn / __fmaf_rn do: the same bits with half the
-// instructions. (Pairs need their operands in aligned register pairs; where
-// the partial sums are many, as in the assoc forms, the register allocator
-// then moves them to local memory, so those forms keep single FMAs.)
-template <typename T, bool FIRST, bool PAIR, int V, class F>
-__device__ __forceinline__ void fma_vec(T (&acc)[V], T c, F a) {
-  if constexpr (PAIR && std::is_same<T, float>::value && V % 2 == 0) {
-    const float2 cc = make_float2(c, c);
-    static_for<V / 2>([&](auto PI) {
-      constexpr int e = 2 * decltype(PI)::value;
-      const float2 av = make_float2(a(IC<e>()), a(IC<e + 1>()));
-      float2 r;
-      if constexpr (FIRST) r = __fmul2_rn(cc, av);
-      else r = __ffma2_rn(cc, av, make_float2(acc[e], acc[e + 1]));
-      acc[e] = r.x;
-      acc[e + 1] = r.y;
-    });
-  } else {
-    static_for<V>([&](auto EI) {
-      constexpr int e = decltype(EI)::value;
-      if constexpr (FIRST) acc[e] = Arith<T>::mul(c, a(EI));
-      else acc[e] = Arith<T>::fma(c, a(EI), acc[e]);
-    });
-  }
 }
 
 // gradient2d.c:17-21: u + num / sqrt(eps + sum_n (u - u_n)^2), evaluated as

@@ -46,6 +46,9 @@ using Occupancy3DFn = int (*)();
 constexpr int kMaxB = 16;
 // warps per CTA of the 2-D kernels (each warp streams its own work items)
 constexpr int kWarpsPerCta2D = 4;
+// largest degree of the 2-D FMA-mode kernels built in stash mode (the
+// adjoint's chunk recompute, which keeps every intermediate state)
+constexpr int kMaxStashB = 4;
 // 3-D block shapes per degree: variant v of the tile kernel has kTileWarps[v]
 // warps (tile rows = warps x rows per warp)
 constexpr int kVar3 = 2;
@@ -53,8 +56,8 @@ constexpr int kTileWarps[kVar3] = {16, 8};
 struct Picks {
   int maxb;
   Launch2DFn l2[kMaxB + 1];
+  Launch2DFn l2s[kMaxB + 1];    // stash-mode 2-D launchers (FMA mode, low degrees; else null)
   Occupancy2DFn o2[kMaxB + 1];
-  int lv2[kMaxB + 1];           // elements per lane of the 2-D launcher (its window is 32 lanes wide)
   Launch3DFn l3[kMaxB + 1][kVar3];
   Occupancy3DFn o3[kMaxB + 1][kVar3];
   int tj3[kMaxB + 1][kVar3];    // tile rows of the 3-D launcher (0: variant not built)

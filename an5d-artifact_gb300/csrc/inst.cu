@@ -82,7 +82,7 @@ template <int B> void add(Picks &p) {
     if constexpr (S::kDim == 2) {
       p.l2[B] = &launch2d<S, T, B, kFma>;
       p.o2[B] = &occupancy2d<S, T, B, kFma>;
-      p.lv2[B] = lane_elems2d<S, T, B, kFma>();
+      if constexpr (kFma && B >= 2 && B <= kMaxStashB) p.l2s[B] = &launch2d<S, T, B, kFma, true>;
     } else {
       add_variant3<B, 0>(p);
       if constexpr (use_tile3d<S, kFma>()) add_variant3<B, 1>(p);

@@ -11,10 +11,8 @@
 // block of output rows [i0, i1) (sl long). It streams level-0 rows
 // i0-b*r .. i1-1+b*r through a per-warp ring of NSTAGE shared-memory row
 // buffers filled by bulk-async (TMA) copies, one 32*V-element window row per
-// copy. Lane l holds window elements [l*V, l*V+V): one 16-byte vector (V =
-// 16 bytes / element size, 512-byte rows) or, in the FMA-mode float kernels
-// of low degree, two (1024-byte rows), which halves the per-row work of the
-// pipeline (waits, copies, shuffles, stores) per cell.
+// copy (V = 16 bytes / element size, 512 bytes per copy). Lane l holds window
+// elements [l*V, l*V+V).
 //
 // Per fused time level l (1..b) the warp keeps a (2r+1)-row register window.
 // At pipeline step p (level-0 row p arrives) level l produces row p - l*r,
@@ -56,8 +54,8 @@ template <typename T, int NT> struct Params2D {
   T coef[NT];
   T div, rdiv, eps;    // divisor, RN(1/divisor), gradient epsilon
   int divmode;         // 0: no division (folded into coef), 1: checked, 2: proven fast path
-  T *stash;            // not null: level l < b also stores its interior cells to stash + (l-1)*stash_stride
-  long long stash_stride;
+  T *stash;            // stash-mode kernels: level l < b also stores its interior cells to
+  long long stash_stride;  // stash + (l-1)*stash_stride (the states between)
 };
 
 // y / div as the params ask (see div_by / div_by_fast)
@@ -116,20 +114,21 @@ template <class ST, int B> constexpr int ring_keep2d() { return ST::kAssoc ? B *
 // ring, which still holds level-0 row q (load index q - pstart). Reading
 // them there costs a shared-memory load instead of a memory round trip in
 // every step of a warp at the grid's edge.
-template <typename T, int NSTAGE, int ROW> struct CarryRing {
+template <typename T, int NSTAGE> struct CarryRing {
   const T *ring;        // the warp's ring + lane * V
   unsigned base;        // the item's first load index on the ring
   int pstart;           // row of load index 0
   int nrows;            // rows loaded by the item
   __device__ __forceinline__ const T *row(int q) const {
     const int n = q - pstart;
-    return (n >= 0 && n < nrows) ? ring + (size_t)((base + (unsigned)n) % NSTAGE) * ROW : nullptr;
+    return (n >= 0 && n < nrows) ? ring + (size_t)((base + (unsigned)n) % NSTAGE) * (32 * (16 / sizeof(T)))
+                                 : nullptr;
   }
 };
 
 template <class ST, typename T, bool FMA, bool UNR, bool CAREFUL, int PH, int V, int NSTAGE>
 __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V], int q, bool edge,
-                                        int col0, const CarryRing<T, NSTAGE, 32 * V> &carry,
+                                        int col0, const CarryRing<T, NSTAGE> &carry,
                                         const Params2D<T, ST::kTerms> &p) {
   constexpr int R = ST::kRad;
   constexpr int W = 2 * R + 1;
@@ -169,22 +168,14 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
           constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
           static_assert(di == 0 || dj == 0, "direct 2-D form expects off-centre rows at dj == 0");
           constexpr int slot = wslot<UNR, W>(PH, R + di);
-          if constexpr (FMA) {
-            fma_vec<T, t == 0, true>(y, p.coef[t], [&](auto EI) -> T {
-              constexpr int e = decltype(EI)::value;
-              if constexpr (dj == 0) return win[slot][e];
-              else return ext[R + e + dj];
-            });
-          } else {
-            static_for<V>([&](auto EI) {
-              constexpr int e = decltype(EI)::value;
-              T a;
-              if constexpr (dj == 0) a = win[slot][e];
-              else a = ext[R + e + dj];
-              if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
-              else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
-            });
-          }
+          static_for<V>([&](auto EI) {
+            constexpr int e = decltype(EI)::value;
+            T a;
+            if constexpr (dj == 0) a = win[slot][e];
+            else a = ext[R + e + dj];
+            if constexpr (t == 0) y[e] = A::mul(p.coef[t], a);
+            else y[e] = term_next<T, FMA>(y[e], p.coef[t], a);
+          });
         });
         if constexpr (ST::kHasDiv && !FMA) {  // FMA mode: folded into the coefficients
 #pragma unroll
@@ -213,17 +204,12 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
       constexpr int t = decltype(TI)::value;
       constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
       constexpr int slot = wslot<UNR, W>(PH, R - di);
-      if constexpr (FMA) {
-        fma_vec<T, t == 0, false>(win[slot], p.coef[t],
-                                  [&](auto EI) -> T { return ext[R + decltype(EI)::value + dj]; });
-      } else {
-        static_for<V>([&](auto EI) {
-          constexpr int e = decltype(EI)::value;
-          const T a = ext[R + e + dj];
-          if constexpr (t == 0) win[slot][e] = A::mul(p.coef[t], a);
-          else win[slot][e] = term_next<T, FMA>(win[slot][e], p.coef[t], a);
-        });
-      }
+      static_for<V>([&](auto EI) {
+        constexpr int e = decltype(EI)::value;
+        const T a = ext[R + e + dj];
+        if constexpr (t == 0) win[slot][e] = A::mul(p.coef[t], a);
+        else win[slot][e] = term_next<T, FMA>(win[slot][e], p.coef[t], a);
+      });
     });
     constexpr int oslot = wslot<UNR, W>(PH, 0);
 #pragma unroll
@@ -262,11 +248,14 @@ __device__ __forceinline__ void level2d(T (&win)[2 * ST::kRad + 1][V], T (&x)[V]
 // warp has issued on them so far, so that items can follow each other on the
 // same barriers. Returns false when a bounded wait gave up (p.err is set and
 // the copies in flight have been drained).
-template <class ST, typename T, int B, bool FMA, int NSTAGE, int LV = 16 / sizeof(T)>
+// STASH: the intermediate levels also store their rows (the states after 1
+// .. B-1 steps) in the item's output rows and columns, where every level is
+// valid, to p.stash; a separate instantiation, so that the plain kernels
+// carry none of it.
+template <class ST, typename T, int B, bool FMA, int NSTAGE, bool STASH = false>
 __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, int strip, int blk, T *ring,
                                             uint64_t *bars, unsigned &load_base) {
-  constexpr int V = LV;                 // elements per lane
-  constexpr int VV = 16 / sizeof(T);    // elements per 16-byte vector
+  constexpr int V = 16 / sizeof(T);
   constexpr int R = ST::kRad;
   constexpr int W = 2 * R + 1;
   constexpr bool UNR = (R <= 2);
@@ -279,7 +268,7 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
   const int cs = R + strip * p.wout;
   const int ce = min(cs + p.wout, p.d1 - R);
   const int need_lo = max(0, cs - B * R);
-  const int ws = ((need_lo + p.shift) / VV) * VV;
+  const int ws = ((need_lo + p.shift) / V) * V;
   const int col0 = ws - p.shift + lane * V;  // column of this lane's element 0
   const bool edge = (ws - p.shift < R) || (ws - p.shift + ROW > p.d1 - R);
   const bool store_all = (col0 >= cs && col0 + V <= ce);
@@ -298,7 +287,7 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
   const unsigned base = load_base;
   constexpr int KEEP = ring_keep2d<ST, B>();
   static_assert(KEEP + 2 <= NSTAGE, "the ring must keep b*r rows and still prefetch");
-  const CarryRing<T, NSTAGE, ROW> carry{ring + lane * V, base, pstart, nload};
+  const CarryRing<T, NSTAGE> carry{ring + lane * V, base, pstart, nload};
 
   if (lane == 0) {
 #pragma unroll 1
@@ -347,11 +336,9 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
     static_for<B>([&](auto LI) {
       constexpr int l = decltype(LI)::value;
       level2d<ST, T, FMA, UNR, careful, ph, V, NSTAGE>(win[l], x, pp - (l + 1) * R, edge, col0, carry, p);
-      if constexpr (l + 1 < B) {
-        // stash mode: this level's row, the state after l+1 steps, in the
-        // item's output rows and columns (valid at every level)
+      if constexpr (STASH && l + 1 < B) {
         const int ql = pp - (l + 1) * R;
-        if (p.stash && ql >= i0 && ql < i1) {
+        if (ql >= i0 && ql < i1) {
           T *d = p.stash + (long long)l * p.stash_stride + ws + lane * V + (long long)ql * pitch;
           if (store_all) {
             st_vec_global<T, V>(d, x);
@@ -429,8 +416,9 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
 }
 
 // The warp's ring and barriers inside the CTA's dynamic shared memory.
-template <typename T, int WPC, int NSTAGE, int ROW = 32 * (16 / sizeof(T))>
+template <typename T, int WPC, int NSTAGE>
 __device__ __forceinline__ void warp_ring2d(unsigned char *smem_raw, T *&ring, uint64_t *&bars) {
+  constexpr int ROW = 32 * (16 / sizeof(T));
   const int wid = threadIdx.x >> 5;
   ring = reinterpret_cast<T *>(smem_raw) + (size_t)wid * NSTAGE * ROW;
   bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)WPC * NSTAGE * ROW * sizeof(T)) + wid * NSTAGE;
@@ -443,7 +431,7 @@ __device__ __forceinline__ void warp_ring2d(unsigned char *smem_raw, T *&ring, u
   __syncwarp();
 }
 
-template <class ST, typename T, int B, bool FMA, int WPC, int NSTAGE, int LV>
+template <class ST, typename T, int B, bool FMA, int WPC, int NSTAGE, bool STASH = false>
 __global__ void __launch_bounds__(WPC * 32, gbs_min_ctas(WPC * 32))
     stencil2d_kernel(const __grid_constant__ Params2D<T, ST::kTerms> p) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -451,61 +439,29 @@ __global__ void __launch_bounds__(WPC * 32, gbs_min_ctas(WPC * 32))
   if (gw >= (long long)p.nstrips * p.nblocks) return;
   T *ring;
   uint64_t *bars;
-  warp_ring2d<T, WPC, NSTAGE, 32 * LV>(smem_raw, ring, bars);
+  warp_ring2d<T, WPC, NSTAGE>(smem_raw, ring, bars);
   unsigned load_base = 0;
-  warp_item2d<ST, T, B, FMA, NSTAGE, LV>(p, (int)(gw % p.nstrips), (int)(gw / p.nstrips), ring, bars, load_base);
+  warp_item2d<ST, T, B, FMA, NSTAGE, STASH>(p, (int)(gw % p.nstrips), (int)(gw / p.nstrips), ring, bars,
+                                            load_base);
 }
 
 constexpr int kWpc2D = kWarpsPerCta2D, kStages2D = 16;
 
-// Elements per lane of the 2-D launcher for (ST, T, B, FMA): two 16-byte
-// vectors in the FMA-mode float kernels whose register windows (B levels of
-// 2r+1 rows) stay small enough, one otherwise.
-template <class ST, typename T, int B, bool FMA>
-constexpr int lane_elems2d() {
-  constexpr int VV = 16 / sizeof(T);
-  return (FMA && sizeof(T) == 4 && ST::kKind != KIND_GRADIENT && B * (2 * ST::kRad + 1) <= 12) ? 2 * VV : VV;
-}
-// ring depth: the same bytes in flight per warp for either row size
-template <class ST, typename T, int B, bool FMA>
-constexpr int stages2d() { return lane_elems2d<ST, T, B, FMA>() == 16 / (int)sizeof(T) ? kStages2D : kStages2D / 2; }
-
-template <class ST, typename T, int B, bool FMA>
-constexpr size_t smem2d() {
-  return (size_t)kWpc2D * stages2d<ST, T, B, FMA>() * (32 * lane_elems2d<ST, T, B, FMA>() * sizeof(T) + sizeof(uint64_t));
-}
-
 template <class ST, typename T, int B, bool FMA>
 int occupancy2d() {
-  constexpr int LV = lane_elems2d<ST, T, B, FMA>(), NS = stages2d<ST, T, B, FMA>();
-  auto kern = stencil2d_kernel<ST, T, B, FMA, kWpc2D, NS, LV>;
-  const size_t smem = smem2d<ST, T, B, FMA>();
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return 0;
-  }
+  constexpr int V = 16 / sizeof(T);
+  const size_t smem = (size_t)kWpc2D * kStages2D * (32 * V * sizeof(T) + sizeof(uint64_t));
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kWpc2D * 32, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stencil2d_kernel<ST, T, B, FMA, kWpc2D, kStages2D>,
+                                                    kWpc2D * 32, smem) != cudaSuccess)
+    return 0;
   return nb * kWpc2D;
 }
 
-template <class ST, typename T, int B, bool FMA>
+template <class ST, typename T, int B, bool FMA, bool STASH = false>
 cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
-  constexpr int WPC = kWpc2D;
-  constexpr int LV = lane_elems2d<ST, T, B, FMA>(), NS = stages2d<ST, T, B, FMA>();
-  auto kern = stencil2d_kernel<ST, T, B, FMA, WPC, NS, LV>;
-  const size_t smem = smem2d<ST, T, B, FMA>();
-  if (smem > 48 * 1024) {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) {
-        (void)cudaGetLastError();
-        return e;
-      }
-      attr_set = true;
-    }
-  }
+  constexpr int WPC = kWpc2D, NSTAGE = kStages2D;
+  constexpr int V = 16 / sizeof(T);
   Params2D<T, ST::kTerms> p;
   p.src = static_cast<const T *>(a.src);
   p.dst = static_cast<T *>(a.dst);
@@ -529,9 +485,11 @@ cudaError_t launch2d(const Launch2D &a, cudaStream_t stream) {
   p.eps = (T)a.eps;
   p.stash = static_cast<T *>(a.stash);
   p.stash_stride = a.stash_stride;
+  if (STASH != (a.stash != nullptr)) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)WPC * NSTAGE * (32 * V * sizeof(T) + sizeof(uint64_t));
   const long long warps = (long long)a.nstrips * a.nblocks;
   const long long grid = (warps + WPC - 1) / WPC;
-  kern<<<(unsigned)grid, WPC * 32, smem, stream>>>(p);
+  stencil2d_kernel<ST, T, B, FMA, WPC, NSTAGE, STASH><<<(unsigned)grid, WPC * 32, smem, stream>>>(p);
   return cudaGetLastError();
 }
 

@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
   constexpr int NS = G::NS, DEP = G::DEP, NPH = G::NPH;
   constexpr size_t PLANE = G::PLANE;
   constexpr bool UNR = G::UNR;
+  using A = Arith<T>;
   using OR = Order3<ST, true>;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -285,8 +286,12 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
             constexpr int h = rho - dj;
             if constexpr (h >= 0 && h < H) {
               constexpr int slot = wslot<UNR, W>(ph, R - di);
-              fma_vec<T, u == OR::init_pos(), false>(acc[l][slot][h], p.coef[t],
-                                               [&](auto EI) -> T { return ext[R + decltype(EI)::value + dk]; });
+              static_for<V>([&](auto EI) {
+                constexpr int e = decltype(EI)::value;
+                const T a = ext[R + e + dk];
+                if constexpr (u == OR::init_pos()) acc[l][slot][h][e] = A::mul(p.coef[t], a);
+                else acc[l][slot][h][e] = A::fma(p.coef[t], a, acc[l][slot][h][e]);
+              });
             }
           });
         }

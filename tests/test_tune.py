@@ -137,18 +137,11 @@ def test_block_shape_choices():
     assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_ERR_UNSUPPORTED
     d, _ = capi.make_desc("star2d1r", np.float32, 256, 10, "fma", bs1=8)
     assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_ERR_UNSUPPORTED
-    # 2-D FMA float: two 16-byte vectors per lane (256 columns) where the
-    # register windows allow (star2d1r up to bt = 4), one (128) beyond
-    for bt, width in ((4, 256), (8, 128)):
-        d, _ = capi.make_desc("star2d1r", np.float32, 256, 10, "fma", bt=bt)
-        pi = capi.PlanInfo()
-        assert L.gbs_plan(ctypes.byref(d), ctypes.byref(pi)) == capi.GBS_OK and pi.bs2 == width
-        d.bs2 = width
-        assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_OK
-        d.bs2 = 384 - width
-        assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_ERR_UNSUPPORTED
+    d, _ = capi.make_desc("star2d1r", np.float32, 256, 10, "fma")
     d.bs2 = 64
     assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_ERR_UNSUPPORTED
+    d.bs2 = 128
+    assert L.gbs_plan(ctypes.byref(d), ctypes.byref(capi.PlanInfo())) == capi.GBS_OK
 
 
 def test_table_records_block_shape(fresh_table):
