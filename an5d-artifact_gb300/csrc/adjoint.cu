@@ -245,20 +245,41 @@ __global__ void __launch_bounds__(kAdjThreads) coef_kernel(const __grid_constant
   }
 }
 
+// The elements of one row that a segment's end lanes cannot take from a
+// neighbouring lane: left[x + R] for x in [-R, 0) (lanes within R/V of the
+// warp's start) and right[x - V] for x in [V, V + R) (lanes within R/V of
+// its end), relative to the lane's first column; loaded once, when the row
+// enters the lane's register window, instead of once per term and use.
+template <typename T, int V, int R> struct RowEdges {
+  T left[R], right[R];
+};
+template <typename T, int V, int R>
+__device__ __forceinline__ void load_edges(RowEdges<T, V, R> &ed, const T *p, long long rowbase, int lane) {
+  static_for<R>([&](auto XI) {
+    constexpr int x = -1 - decltype(XI)::value;  // -1 .. -R
+    constexpr int dl = (-x + V - 1) / V;
+    if (lane < dl) ed.left[x + R] = p[rowbase + x];
+  });
+  static_for<R>([&](auto XI) {
+    constexpr int x = V + decltype(XI)::value;   // V .. V+R-1
+    constexpr int dl = x / V;
+    if (lane >= 32 - dl) ed.right[x - V] = p[rowbase + x];
+  });
+}
 // Element x (relative to the lane's first column, x in [-R, V+R)) of row
-// offset D of a plane whose 2R+1 row vectors the lane holds: from its own
-// vector or from a lane up to R/V away; lanes whose source lane lies outside
-// the warp load the element.
+// offset D of the lane's 2R+1-row window: from its own vector, from a lane up
+// to R/V away, or, for the lanes whose source lane lies outside the warp,
+// from the row's cached edges
 template <int V, int R, int D, int X, typename T>
-__device__ __forceinline__ T row_value(const T *p, const T (&rows)[2 * R + 1][V], long long base, long long pitch,
-                                       int lane) {
+__device__ __forceinline__ T row_value_cached(const T (&rows)[2 * R + 1][V], const RowEdges<T, V, R> (&ed)[2 * R + 1],
+                                              int lane) {
   T v = row_elem<V, X>(rows[D + R]);
   if constexpr (X < 0) {
     constexpr int dl = (-X + V - 1) / V;
-    if (lane < dl) v = p[base + (long long)D * pitch + X];
+    if (lane < dl) v = ed[D + R].left[X + R];
   } else if constexpr (X >= V) {
     constexpr int dl = X / V;
-    if (lane >= 32 - dl) v = p[base + (long long)D * pitch + X];
+    if (lane >= 32 - dl) v = ed[D + R].right[X - V];
   }
   return v;
 }
@@ -314,10 +335,16 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
     const long long col = (long long)g.shift + c0;
     // windows of rows i-R .. i+R (position d+R holds row i+d)
     T lw[W][V], uw[W][V];
+    RowEdges<T, V, R> le[W], ue[W];  // the segment-end elements of each window row
     static_for<W - 1>([&](auto DI) {
       constexpr int d = decltype(DI)::value - R;  // rows ia-R .. ia+R-1
-      ld_vec<T, V>(lw[d + R + 1], lam + (long long)(ia + d) * g.pitch + col);
-      if constexpr (WANT_COEF) ld_vec<T, V>(uw[d + R + 1], u + (long long)(ia + d) * g.pitch + col);
+      const long long rb = (long long)(ia + d) * g.pitch + col;
+      ld_vec<T, V>(lw[d + R + 1], lam + rb);
+      load_edges<T, V, R>(le[d + R + 1], lam, rb, lane);
+      if constexpr (WANT_COEF) {
+        ld_vec<T, V>(uw[d + R + 1], u + rb);
+        load_edges<T, V, R>(ue[d + R + 1], u, rb, lane);
+      }
     });
 #pragma unroll 1
     for (int i = ia; i < ib; ++i) {
@@ -329,10 +356,16 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
           lw[d][e] = lw[d + 1][e];
           if constexpr (WANT_COEF) uw[d][e] = uw[d + 1][e];
         }
+        le[d] = le[d + 1];
+        if constexpr (WANT_COEF) ue[d] = ue[d + 1];
       });
       const long long base = (long long)i * g.pitch + col;
       ld_vec<T, V>(lw[W - 1], lam + base + (long long)R * g.pitch);
-      if constexpr (WANT_COEF) ld_vec<T, V>(uw[W - 1], u + base + (long long)R * g.pitch);
+      load_edges<T, V, R>(le[W - 1], lam, base + (long long)R * g.pitch, lane);
+      if constexpr (WANT_COEF) {
+        ld_vec<T, V>(uw[W - 1], u + base + (long long)R * g.pitch);
+        load_edges<T, V, R>(ue[W - 1], u, base + (long long)R * g.pitch, lane);
+      }
       T sv[V];
 #pragma unroll
       for (int e = 0; e < V; ++e) sv[e] = T(0);
@@ -341,7 +374,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
         constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
         static_for<V>([&](auto EI) {
           constexpr int e = decltype(EI)::value;
-          sv[e] = fma(cf.c[t], row_value<V, R, -di, e - dj>(lam, lw, base, g.pitch, lane), sv[e]);
+          sv[e] = fma(cf.c[t], row_value_cached<V, R, -di, e - dj>(lw, le, lane), sv[e]);
         });
       });
       if constexpr (WANT_COEF) {
@@ -350,7 +383,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
           constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
           static_for<V>([&](auto EI) {
             constexpr int e = decltype(EI)::value;
-            const T uv = row_value<V, R, di, e + dj>(u, uw, base, g.pitch, lane);
+            const T uv = row_value_cached<V, R, di, e + dj>(uw, ue, lane);
             if (e < nvalid) acc[t] = fma(lw[R][e], uv, acc[t]);
           });
         });

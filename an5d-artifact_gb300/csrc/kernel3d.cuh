@@ -459,15 +459,31 @@ constexpr int tile_wk3d() {
   return use_tile3d<ST, FMA>() ? TileOf<ST, T, B, NW>::WK : (32 * V - 2 * B * ST::kRad - (V - 1)) / V * V;
 }
 
+// Double at degree 1 runs the tile as a decoupled pipeline (one producer
+// warp more): the FP64 pipe bounds it, and the per-plane barrier of the tile
+// kernel idles that pipe while the last warps of a plane drain. (Float at
+// degree 1 is bound by HBM; with the extra warp its registers would spill.)
+template <class ST, typename T, int B, bool FMA>
+constexpr bool use_stream3d() { return use_tile3d<ST, FMA>() && B == 1 && sizeof(T) == 8; }
+
 template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 constexpr size_t smem_bytes3d() {
-  if constexpr (use_tile3d<ST, FMA>()) return TileOf<ST, T, B, NW>::bytes();
-  else return Smem3<ST, T, FMA>::bytes(kTj3D, B);
+  if constexpr (use_stream3d<ST, T, B, FMA>()) {
+    using G = TileOf<ST, T, B, NW>;
+    return Stream3<ST, T, NW, rows_per_warp<ST, T, B>(), G::NS>::bytes();
+  } else if constexpr (use_tile3d<ST, FMA>()) {
+    return TileOf<ST, T, B, NW>::bytes();
+  } else {
+    return Smem3<ST, T, FMA>::bytes(kTj3D, B);
+  }
 }
 
 template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 auto kernel3d_ptr() {
-  if constexpr (use_tile3d<ST, FMA>()) {
+  if constexpr (use_stream3d<ST, T, B, FMA>()) {
+    using G = TileOf<ST, T, B, NW>;
+    return stencil3d_stream_kernel<ST, T, NW, rows_per_warp<ST, T, B>(), G::NS>;
+  } else if constexpr (use_tile3d<ST, FMA>()) {
     using G = TileOf<ST, T, B, NW>;
     return stencil3d_tile_kernel<ST, T, B, NW, rows_per_warp<ST, T, B>(), G::NS>;
   } else {
@@ -476,7 +492,9 @@ auto kernel3d_ptr() {
 }
 
 template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
-constexpr int threads3d() { return use_tile3d<ST, FMA>() ? NW * 32 : kTj3D * 32; }
+constexpr int threads3d() {
+  return use_tile3d<ST, FMA>() ? (use_stream3d<ST, T, B, FMA>() ? NW + 1 : NW) * 32 : kTj3D * 32;
+}
 
 template <class ST, typename T, int B, bool FMA, int NW = kNw3D>
 cudaError_t launch3d(const Launch3D &a, cudaStream_t stream) {

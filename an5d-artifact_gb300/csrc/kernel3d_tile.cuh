@@ -372,4 +372,185 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
   }
 }
 
+// ---------------------------------------------------------------------------
+// Degree 1: the same tile, as a decoupled pipeline. With no intermediate
+// level, the only thing the tile kernel's per-plane __syncthreads protects
+// is the reuse of a ring stage, and that barrier makes every warp wait for
+// the slowest before the next plane (on the FP64 pipe, whose throughput is
+// the bound, the pipe then idles while the last warps drain). Here one extra
+// warp is the producer: for each plane it waits (bounded) on the stage's
+// "empty" mbarrier, on which every consumer warp arrives once it has read
+// the plane, then issues the tensor copy whose bytes complete the stage's
+// "full" mbarrier. Consumer warps wait (bounded) on "full" only, so they run
+// up to NS-1 planes apart and the pipe always has work. Every wait is
+// bounded; a consumer that gives up stops, and the producer, which then
+// finds its stage never released, gives up too and waits (bounded) for its
+// copies in flight before the CTA exits.
+// ---------------------------------------------------------------------------
+template <class ST, typename T, int NW, int H, int NSTAGE>
+struct Stream3 {
+  using G = Tile3<ST, T, 1, NW, H, NSTAGE>;
+  static constexpr size_t bytes() { return G::PLANE * G::NS + 2 * G::NS * sizeof(uint64_t); }
+};
+
+template <class ST, typename T, int NW, int H, int NSTAGE>
+__global__ void __launch_bounds__((NW + 1) * 32, gbs_min_ctas((NW + 1) * 32))
+    stencil3d_stream_kernel(const __grid_constant__ Params3T<T, ST::kTerms> p) {
+  using G = Tile3<ST, T, 1, NW, H, NSTAGE>;
+  static_assert(G::valid(), "a tensor-map box is at most 256 elements per axis, and the tile needs outputs");
+  constexpr int V = G::V, R = G::R, W = G::W, BX = G::BX, PADE = G::PADE;
+  constexpr int NS = G::NS, NPH = G::NPH;
+  constexpr size_t PLANE = G::PLANE;
+  constexpr bool UNR = G::UNR;
+  using OR = Order3<ST, true>;
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *ring0 = smem_raw;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + NS * PLANE);
+  uint64_t *empty = full + NS;
+
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  int bid = blockIdx.x;
+  const int tk = bid % p.ntk;
+  bid /= p.ntk;
+  const int tj = bid % p.ntj;
+  const int blk = bid / p.ntj;
+
+  const int cs = R + tk * p.wk;
+  const int ce = min(cs + p.wk, p.d2 - R);
+  const int ws = p.shift + cs;  // element index of the window's column 0 (a multiple of V)
+  const int col0 = ws - p.shift + lane * V;
+  const bool store_all = (col0 >= cs && col0 + V <= ce);
+  const int js = R + tj * p.jout;
+  const int je = min(js + p.jout, p.d1 - R);
+  const int j0 = js + w * H;
+  const int i0 = R + blk * p.sl;
+  const int i1 = min(i0 + p.sl, p.d0 - R);
+  const int pstart = max(0, i0 - R);
+  const int pend = min(p.d0, i1 + R);
+  const int slast = i1 - 1 + R;
+  const long long plane_stride = (long long)p.d1 * p.pitch;
+
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NW);
+    }
+    fence_mbar_init();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+
+  if (w == NW) {
+    // producer warp: lane 0 issues every plane of the block
+    if (lane == 0) {
+      int issued = pstart;
+      for (int pl = pstart; pl < pend; ++pl) {
+        const int n = pl - pstart;
+        const int st = n % NS;
+        // the stage's previous plane (n - NS) must have been read by every consumer
+        if (n >= NS && !mbar_wait(&empty[st], (unsigned)((n / NS) - 1) & 1u, p.err, ERR_WAIT_TIMEOUT)) break;
+        mbar_arrive_expect_tx(&full[st], (unsigned)G::BOX_BYTES);
+        tma_load_3d(ring0 + (size_t)st * PLANE, &p.tmap, ws - PADE, js - R, pl, &full[st]);
+        issued = pl + 1;
+      }
+      // the last copy of each stage has landed before the CTA may exit
+      for (int n = max(0, issued - pstart - NS); n < issued - pstart; ++n)
+        if (!mbar_wait(&full[n % NS], (unsigned)(n / NS) & 1u, p.err, ERR_DRAIN_TIMEOUT)) break;
+    }
+    return;
+  }
+
+  T acc[W][H][V];
+  static_for<W>([&](auto AI) {
+    static_for<H>([&](auto HI) {
+      static_for<V>([&](auto EI) { acc[decltype(AI)::value][decltype(HI)::value][decltype(EI)::value] = T(0); });
+    });
+  });
+
+  bool ok = true;
+  auto step = [&](auto PHI, int s) {
+    constexpr int ph = decltype(PHI)::value;
+    const int n = s - pstart;
+    const int st = n % NS;
+    if (s < pend) {
+      const bool got = mbar_wait(&full[st], (unsigned)(n / NS) & 1u, nullptr, 0);
+      if (!__all_sync(0xffffffffu, got)) {
+        if (lane == 0) atomicOr(p.err, ERR_WAIT_TIMEOUT);
+        ok = false;
+        return;
+      }
+    }
+    // past the block's last plane the stage holds an older plane: its terms
+    // reach only outputs that are not stored
+    const T *in_m = reinterpret_cast<const T *>(ring0 + (size_t)st * PLANE);
+    const int q = s - R;
+    static_for<H + 2 * R>([&](auto RI) {
+      constexpr int rho = decltype(RI)::value - R;
+      using Need = RowNeed<ST, rho, H, V>;
+      if constexpr (Need::used()) {
+        T ext[V + 2 * R];
+        load_ext<T, V, R, Need>(ext, in_m + (size_t)(w * H + R + rho) * BX + PADE + lane * V);
+        static_for<ST::kTerms>([&](auto UI) {
+          constexpr int u = decltype(UI)::value;
+          constexpr int t = OR::idx.v[u];
+          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1], dk = ST::kOff[t][2];
+          constexpr int h = rho - dj;
+          if constexpr (h >= 0 && h < H) {
+            constexpr int slot = wslot<UNR, W>(ph, R - di);
+            static_for<V>([&](auto EI) {
+              constexpr int e = decltype(EI)::value;
+              const T a = ext[R + e + dk];
+              if constexpr (u == OR::init_pos()) acc[slot][h][e] = Arith<T>::mul(p.coef[t], a);
+              else acc[slot][h][e] = Arith<T>::fma(p.coef[t], a, acc[slot][h][e]);
+            });
+          }
+        });
+      }
+    });
+    // every lane of the warp has read the plane: release the stage
+    __syncwarp();
+    if (s < pend && lane == 0) mbar_arrive(&empty[st]);
+    constexpr int oslot = wslot<UNR, W>(ph, 0);
+    if (q >= i0 && q < i1) {
+      static_for<H>([&](auto HI) {
+        constexpr int h = decltype(HI)::value;
+        const int jr = j0 + h;
+        if (jr >= js && jr < je) {
+          T *d = p.dst + q * plane_stride + (long long)jr * p.pitch + ws + lane * V;
+          if (store_all) {
+            st_vec_global<T, V>(d, acc[oslot][h]);
+          } else {
+            static_for<V>([&](auto EI) {
+              constexpr int e = decltype(EI)::value;
+              if (col0 + e >= cs && col0 + e < ce) st_global(d + e, acc[oslot][h][e]);
+            });
+          }
+        }
+      });
+    }
+    if constexpr (!UNR) {
+      static_for<2 * R>([&](auto AI) {
+        constexpr int a = decltype(AI)::value;
+        static_for<H>([&](auto HI) {
+          static_for<V>([&](auto EI) {
+            acc[a][decltype(HI)::value][decltype(EI)::value] = acc[a + 1][decltype(HI)::value][decltype(EI)::value];
+          });
+        });
+      });
+    }
+  };
+
+#pragma unroll 1
+  for (int sb = pstart; ok && sb <= slast; sb += NPH) {
+    static_for<NPH>([&](auto PHI) {
+      const int s = sb + decltype(PHI)::value;
+      if (!ok || s > slast) return;
+      step(PHI, s);
+    });
+  }
+}
+
 }  // namespace gbs
