@@ -73,7 +73,7 @@ BATCH_MIX = ["star2d1r", "star2d2r", "star2d3r", "star2d4r", "box2d1r", "box2d2r
 # once, so traffic grows in proportion). Keyed by (stencil, dtype, bt); the
 # value names the capture, whose summary is under profiles/.
 NCU_DRAM_BYTES_PER_CELL = {
-    ("box3d1r", "float64", 1): (14.80, "profiles/stencil3d_tile_box3d1r_f64_n256.md (256^3 capture)"),
+    ("box3d1r", "float64", 1): (15.01, "profiles/stencil3d_stream_box3d1r_f64_n256.md (256^3 capture)"),
     ("star3d2r", "float32", 1): (9.01, "profiles/stencil3d_tile_star3d2r_f32_n320.md (320^3 capture)"),
 }
 
