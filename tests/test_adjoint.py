@@ -335,3 +335,46 @@ def test_adjoint_workspace_size(name, dtype, n, T, C):
     # the 16 GB budget of the gradient2d configuration holds
     if name == "gradient2d":
         assert nbytes.value < 16e9
+
+
+@pytest.mark.gpu
+def test_adjoint_gradient_at_configuration_size():
+    """j2d5pt float32 at the adjoint configuration's size (2048^2, T=1024,
+    checkpoints every 32, loss 0.5 |u_T - target|^2, gradients of u_0 and of
+    the five coefficients): directional derivatives of the engine's float32
+    adjoint against Richardson-extrapolated central differences of the
+    engine's float64 forward loop, relative error <= 1e-4."""
+    import torch
+    from gbstencil.adjoint import Checkpointed
+    name, n, T, C = "j2d5pt", 2048, 1024, 32
+    r = ar.BY_NAME[name]["rad"]
+    shape = [n + 2 * r] * 2
+    rng = RNG(31)
+    u0 = rng.random(shape).astype(np.float32).astype(np.float64)
+    target = rng.random(shape)
+    coef = ar.default_coef(name)
+    inner = (slice(r, -r), slice(r, -r))
+    run = Checkpointed(name, torch.tensor(u0, dtype=torch.float32, device="cuda"), T, C)
+    lam = (run.u_T.double() - torch.tensor(target, device="cuda")).float()
+    gu, gc = run.backward(lam, want_coef=True)
+    torch.cuda.synchronize()
+    gu, gc = gu.double().cpu().numpy(), gc.cpu().numpy()
+    tgt = torch.tensor(target[inner], device="cuda")
+
+    def loss(u, c):
+        # forward only: one checkpoint, no stash planes
+        f = Checkpointed(name, torch.tensor(u, device="cuda"), T, T, coef=c, slots=0)
+        torch.cuda.synchronize()
+        return float(0.5 * ((f.u_T[inner] - tgt) ** 2).sum())
+
+    def richardson(f, h):
+        d1 = (f(h) - f(-h)) / (2 * h)
+        d2 = (f(h / 2) - f(-h / 2)) / h
+        return (4 * d2 - d1) / 3
+
+    du = RNG(32).standard_normal(shape)
+    fd = richardson(lambda e: loss(u0 + e * du, coef), 1e-3)
+    assert abs(fd - np.sum(gu * du)) <= 1e-4 * abs(fd), (fd, np.sum(gu * du))
+    dc = RNG(33).standard_normal(coef.shape)
+    fd = richardson(lambda e: loss(u0, coef + e * dc), 1e-5)
+    assert abs(fd - np.sum(gc * dc)) <= 1e-4 * abs(fd), (fd, np.sum(gc * dc))
