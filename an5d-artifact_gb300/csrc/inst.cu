@@ -38,14 +38,16 @@ constexpr int wk_pick(int b, std::integer_sequence<int, Bs...>) {
   ((r = (Bs + 1 == b) ? tile_wk3d<S, T, Bs + 1, kFma>() : r), ...);
   return r;
 }
-constexpr int kMax3D = 4;  // largest 3-D degree considered
+constexpr int kMax3D = 8;  // largest 3-D degree considered
 constexpr size_t smem_bytes3d_b(int b) { return smem_pick(b, std::make_integer_sequence<int, kMax3D>()); }
 constexpr int jout_b(int b) { return jout_pick(b, std::make_integer_sequence<int, kMax3D>()); }
 constexpr int wk_b(int b) { return wk_pick(b, std::make_integer_sequence<int, kMax3D>()); }
 
 // Exact mode spends two FP instructions per term, so its best degree is
-// lower; it keeps degrees up to 4. In 3-D a tile of 32 rows loses 2*b*r rows
-// to overlap, and FP64 is compute-bound from b=1.
+// lower; it keeps degrees up to 4. In 3-D a tile loses 2*(b-1)*r of its rows
+// and (b-1)*r of its columns to overlap, and FP64 is compute-bound from b=1;
+// FMA mode still builds every degree up to 8 whose tile fits and keeps
+// outputs, so that the whole degree range can be measured.
 constexpr int max_class() {
   if (!kFma && !S::kExact) return 0;  // no exact form (3d125pt: float group sums combined in double)
   if (S::kDim == 2) {
@@ -56,7 +58,7 @@ constexpr int max_class() {
     return S::kRad <= 2 ? cap : 4;
   }
   if (S::kRad >= 3) return 1;
-  int b = sizeof(T) == 8 ? 2 : (S::kRad == 1 ? 4 : 3);
+  int b = kFma ? kMax3D : (sizeof(T) == 8 ? 2 : (S::kRad == 1 ? 4 : 3));
   // the level rings must fit the 227 KB of shared memory a CTA may use, and
   // the tile must keep output rows and columns after the overlap
   while (b > 1 && (smem_bytes3d_b(b) > 227u * 1024u || jout_b(b) <= 0 || wk_b(b) <= 0)) --b;

@@ -3,6 +3,7 @@
     python -m gbstencil.report run    --prec float  --out gb300      # compiled/run.sh
     python -m gbstencil.report sconf  --out gb300                    # run_sconf.sh
     python -m gbstencil.report regcap --caps 0,32,64,96 --out gb300  # all.sh REGNUM loop
+    python -m gbstencil.report sweep  -t 100 --out gb300             # make.sh --bt, 1..8
 
 ``run`` writes ``<out>/<prec>_run.csv`` in the format of compiled/run.sh
 (compiled/run.sh:14,35,58): ``Stencil,bS1,bS2,bT,sl,Model,Measured`` with one
@@ -18,6 +19,15 @@ tile rows x tile columns; Model is the autotuner's roofline model for it.
 ``sconf`` repeats run_sconf.sh's fixed configuration (make_sconf.sh: bt=4,
 bs1=128 for 2-D, 32x32 with sl=512 for 3-D) for its seven stencils, in float
 and double, with bt clamped to the largest fused degree the build has.
+
+``sweep`` times every fused degree bt = 1 .. --bt-max that the build has
+for each stencil of --stencils (default star3d2r,box3d1r) in float and
+double at -s (3-D: --s3), the degree sweep of the artifact's make.sh --bt
+option; the grid stays on the device and each of -n runs is timed with CUDA
+events. It writes ``<out>/sweep.csv``: Stencil, Precision, bT, bS1, bS2,
+sl, redundancy (computed cells per output cell), Model and Measured GCells/s,
+and Measured as a share of Roofline(bt) = min(HBM * bt / (2 * element
+bytes), FP peak / flops per cell) with the measured peaks.
 
 ``regcap`` runs ``run`` once per register cap (0 = none), each with the
 library built by ``python -m gbstencil.build --regcap=N``, and writes
@@ -133,6 +143,72 @@ def max_degree(name, dtype, mode):
     return top
 
 
+def copy_bandwidth(nbytes=2 << 30, reps=5):
+    """Device-to-device copy bandwidth (bytes read + written per second) of
+    the current GPU, the HBM roof of the sweep's Roofline(bt)."""
+    import torch
+    src = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda").fill_(1.0)
+    dst = torch.empty_like(src)
+    dst.copy_(src)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        dst.copy_(src)
+    e1.record()
+    e1.synchronize()
+    bw = 2.0 * nbytes * reps / (e0.elapsed_time(e1) * 1e-3)
+    del src, dst
+    torch.cuda.empty_cache()
+    return bw
+
+
+def cmd_sweep(args):
+    import torch
+    from .grid import DeviceGrid
+    out = Path(args.out)
+    out.mkdir(parents=True, exist_ok=True)
+    names = args.stencils.split(",") if args.stencils else ["star3d2r", "box3d1r"]
+    hbm = copy_bandwidth()
+    path = out / "sweep.csv"
+    with open(path, "w", newline="") as f:
+        w = csv.writer(f)
+        w.writerow(["Stencil", "Precision", "bT", "bS1", "bS2", "sl", "Redundancy", "Model GCells/s",
+                    "Measured GCells/s", "Roofline(bt) GCells/s", "% of Roofline(bt)"])
+        for name in names:
+            s = capi.info(name)
+            n = args.s2 if s["dim"] == 2 else args.s3
+            cells = float(n) ** s["dim"] * args.t
+            for prec in ("float", "double"):
+                dt = PREC[prec]
+                fp = capi.measure_fp_peak(dt) * 1e9
+                g = DeviceGrid(name, dt, [n] * s["dim"])
+                g.fill_uniform(1)
+                for bt in range(1, min(args.bt_max, max_degree(name, dt, args.mode)) + 1):
+                    d, _ = g.desc(args.t, args.mode, bt=bt)
+                    p = capi.plan(d)
+                    model_ms = ctypes.c_double(0.0)
+                    capi.check(capi.lib().gbs_tune_model(ctypes.byref(d), ctypes.byref(model_ms)))
+                    g.run(args.t, args.mode, bt=bt)  # warm-up
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    for _ in range(args.n):
+                        g.run(args.t, args.mode, bt=bt)
+                    e1.record()
+                    e1.synchronize()
+                    meas = cells * args.n / (e0.elapsed_time(e1) * 1e-3) / 1e9
+                    model = cells / (model_ms.value * args.t * 1e-3) / 1e9
+                    roof = min(hbm * bt / (2 * np.dtype(dt).itemsize), fp / s["fpp"]) / 1e9
+                    w.writerow([name, prec, p.bt, p.bs1, p.bs2, p.sl, f"{p.redundancy:.3f}", f"{model:.1f}",
+                                f"{meas:.1f}", f"{roof:.1f}", f"{100 * meas / roof:.1f}"])
+                    f.flush()
+                    print(f"{name:9s} {prec:6s} bT={p.bt} bS1={p.bs1} sl={p.sl} red {p.redundancy:.2f} "
+                          f"measured {meas:8.1f} GCells/s ({100 * meas / roof:5.1f}% of Roofline(bt) "
+                          f"{roof:.0f})", flush=True)
+                del g
+                torch.cuda.empty_cache()
+    return path
+
+
 def cmd_regcap(args):
     from . import build as gb
     out = Path(args.out)
@@ -159,7 +235,7 @@ def cmd_regcap(args):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("what", choices=["run", "sconf", "regcap"])
+    ap.add_argument("what", choices=["run", "sconf", "regcap", "sweep"])
     ap.add_argument("--prec", default="float", choices=list(PREC))
     ap.add_argument("--out", default="gb300")
     ap.add_argument("--stencils", default="")
@@ -169,8 +245,9 @@ def main(argv=None):
     ap.add_argument("--s2", type=int, default=16384, help="2-D compute size (-s)")
     ap.add_argument("--s3", type=int, default=512, help="3-D compute size (-s)")
     ap.add_argument("--caps", default="0,32,64,96")
+    ap.add_argument("--bt-max", type=int, default=8, help="sweep: largest fused degree")
     args = ap.parse_args(argv)
-    path = {"run": cmd_run, "sconf": cmd_sconf, "regcap": cmd_regcap}[args.what](args)
+    path = {"run": cmd_run, "sconf": cmd_sconf, "regcap": cmd_regcap, "sweep": cmd_sweep}[args.what](args)
     print(path)
 
 

@@ -35,7 +35,7 @@ def max_class(name, dt, mode):
     s = capi.info(name)
     if mode == "exact" and not has_exact(name):
         return 0
-    if s.get("groups"):  # degrees limited by shared memory: ask the planner
+    if s.get("groups") or s["dim"] == 3:  # degrees limited by shared memory: ask the planner
         import ctypes
         top = 0
         for bt in range(1, 9):
@@ -44,14 +44,6 @@ def max_class(name, dt, mode):
                 break
             top = bt
         return top
-    if s["dim"] == 3:
-        if s["rad"] >= 3:
-            return 1
-        if np.dtype(dt) == np.float64:
-            return 2
-        if mode == "exact" and s["form"] == "direct" and s["rad"] == 2:
-            return 2  # shared-memory bound of the direct form's plane rings
-        return 4 if s["rad"] == 1 else 3
     if np.dtype(dt) == np.float64:
         return 2
     if s["kind"] == "gradient":
@@ -181,7 +173,7 @@ def test_parity_3d(name, dt, mode):
         return
     seed = 100
     for n, T, sl in CASES_3D:
-        for bt in sorted({1, mc, 2 if mc >= 2 else 1}):
+        for bt in sorted({1, mc, min(2, mc), max(1, mc // 2)}):
             seed += 1
             A0, nn = random_grid(name, n, dt, seed)
             compare(name, A0, nn, T, dt, mode, bt, sl=sl)

@@ -8,10 +8,24 @@ from gbstencil import capi, report
 
 
 def test_max_degree_matches_plan():
-    # 3-D radius >= 3 kernels are built for one fused step only; 2-D stars to 8 (FMA)
+    # 3-D radius >= 3 kernels are built for one fused step only; 2-D stars to 8
+    # (FMA); 3-D FMA tiles to 8 while they keep output rows, exact mode to 2-4
     assert report.max_degree("star3d3r", np.float32, "fma") == 1
     assert report.max_degree("star2d1r", np.float32, "fma") == 8
-    assert report.max_degree("j3d27pt", np.float64, "fma") == 2
+    assert report.max_degree("j3d27pt", np.float64, "fma") == 8
+    assert report.max_degree("star3d2r", np.float32, "fma") == 4
+    assert report.max_degree("j3d27pt", np.float64, "exact") == 2
+    assert report.max_degree("box3d1r", np.float32, "exact") == 4
+
+
+@pytest.mark.gpu
+def test_sweep_csv(tmp_path):
+    report.main(["sweep", "--out", str(tmp_path), "-t", "4", "-n", "1", "--s3", "48", "--stencils", "star3d2r",
+                 "--bt-max", "2"])
+    rows = list(csv.reader(open(tmp_path / "sweep.csv")))
+    assert rows[0][:3] == ["Stencil", "Precision", "bT"]
+    assert [(r[1], r[2]) for r in rows[1:]] == [("float", "1"), ("float", "2"), ("double", "1"), ("double", "2")]
+    assert all(float(r[8]) > 0 for r in rows[1:])
 
 
 def test_sconf_stencils_are_the_papers_seven():

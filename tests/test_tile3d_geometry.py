@@ -88,7 +88,10 @@ def check(R, V, B, TJ, H, n, sl):
 
 SHAPES = [(1, 4, 1, 64, 4), (2, 4, 1, 64, 4), (1, 4, 2, 64, 4), (1, 4, 3, 32, 2), (1, 4, 4, 32, 2),
           (2, 4, 2, 32, 2), (2, 4, 3, 16, 1), (1, 2, 1, 64, 4), (2, 2, 1, 64, 4), (1, 2, 2, 64, 4),
-          (2, 2, 2, 32, 2), (3, 4, 1, 16, 1), (4, 2, 1, 16, 1), (3, 2, 2, 16, 1)]
+          (2, 2, 2, 32, 2), (3, 4, 1, 16, 1), (4, 2, 1, 16, 1), (3, 2, 2, 16, 1),
+          # the high degrees of FMA mode: one row per warp, few output rows
+          (1, 4, 5, 16, 1), (1, 4, 8, 16, 1), (1, 2, 6, 16, 1), (1, 2, 8, 16, 1), (2, 4, 4, 16, 1),
+          (2, 2, 4, 16, 1)]
 
 
 @pytest.mark.parametrize("R,V,B,TJ,H", SHAPES)
