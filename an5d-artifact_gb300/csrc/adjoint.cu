@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(kAdjThreads) grad_adj_kernel(const __grid_cons
   double pnum = 0.0;
   if (cidx < g.cells) {
     const int i = (int)(cidx / g.d1), j = (int)(cidx - (long long)(cidx / g.d1) * g.d1);
-    auto inter = [&](int a, int b) { return a >= R && a < g.d0 - R && b >= R && b < g.d1 - R; };
+    auto inter = [&](int a, int b) GBS_INL { return a >= R && a < g.d0 - R && b >= R && b < g.d1 - R; };
     const long long o = cell_off(g, i, j, 0);
     const bool yin = inter(i, j);
     T acc = T(0);

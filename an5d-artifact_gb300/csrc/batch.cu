@@ -42,6 +42,10 @@ struct GridDev {
   long long pitch, plane;
   int d0, d1, shift, sid;
   int sl, nblocks;
+  // completion counters of the grid: done[cbase .. cbase + ccount); one per
+  // stream block (an item waits for its own block and the two beside it),
+  // or one for the whole grid (an item waits for every earlier item of it)
+  int cbase, ccount;
   float coef[kMaxTerms];
   float div, rdiv, eps;
   int divmode;
@@ -57,6 +61,14 @@ using batchdetail::Item;
 namespace {
 constexpr bool kFma = GBS_FMA != 0;
 constexpr int kWpc = kWpc2D, kStages = kStages2D;
+// CTAs per SM the batched kernels are built for. The layered kernel takes 4
+// (at most 128 registers a thread, 16 warps an SM; every variant but
+// star2d3r at degree 2 fits without spilling): 2.92x the per-grid launches
+// on the 512-grid mix against 2.76x at 3 CTAs (168 registers, of which the
+// heaviest variants use 154-164 and so set them for all). The persistent
+// kernel keeps 3: at 4 its warps stalled more on instruction fetch (more
+// variants resident per SM) and it was 1% slower.
+constexpr int kLayerCtas = 4, kPersistentCtas = 3;
 
 // The stencils a batch may mix and the fused degree used for each (the full
 // blocks; remainders run at degree 1).
@@ -72,8 +84,8 @@ struct Args {
   const GridDev *grids;
   const Item *items;
   int nitems;
-  unsigned *next;       // work counter
-  unsigned *done;       // per-grid completed items
+  unsigned *next;       // groups of kWpc items taken (persistent)
+  unsigned *done;       // completed items per counter (GridDev::cbase)
   int *err;
 };
 
@@ -92,15 +104,20 @@ static_assert(sizeof(Params2D<float, batchdetail::kMaxTerms>) <= kParamSlot, "pa
 // forces a local-memory frame onto every variant's loop) and the call costs
 // once per item. The parameters (with up to 81 coefficients) are staged in
 // shared memory: a per-thread copy would sit on the local-memory stack.
+// Everything else comes by value (time block k, strip, stream block, the
+// warp's copy count) and the new copy count is the return value, ~0u when a
+// bounded wait gave up: a reference into the caller's frame would place
+// that frame in local memory.
 template <class S, int B>
-__device__ __noinline__ bool run_item(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
-                                      unsigned &load_base, int *err, unsigned char *slot) {
+__device__ __noinline__ unsigned run_item(const GridDev *gp, int k, int strip, int blk, float *ring,
+                                          uint64_t *bars, unsigned load_base, int *err, unsigned char *slot) {
+  const GridDev &g = *gp;
   auto &p = *reinterpret_cast<Params2D<float, S::kTerms> *>(slot);
   const int lane = threadIdx.x & 31;
   for (int t = lane; t < S::kTerms; t += 32) p.coef[t] = g.coef[t];
   if (lane == 0) {
-    p.src = g.base + (long long)(it.k % 2) * g.plane;
-    p.dst = g.base + (long long)((it.k + 1) % 2) * g.plane;
+    p.src = g.base + (long long)(k % 2) * g.plane;
+    p.dst = g.base + (long long)((k + 1) % 2) * g.plane;
     p.err = err;
     p.pitch = g.pitch;
     p.d0 = g.d0;
@@ -123,23 +140,26 @@ __device__ __noinline__ bool run_item(const GridDev &g, const Item &it, float *r
   if constexpr (S::kTerms <= 25) {
     // small parameter sets ride in registers for the whole item
     const Params2D<float, S::kTerms> pl = p;
-    ok = warp_item2d<S, float, B, kFma, kStages>(pl, it.strip, it.blk, ring, bars, load_base);
+    ok = warp_item2d<S, float, B, kFma, kStages>(pl, strip, blk, ring, bars, load_base);
   } else {
-    ok = warp_item2d<S, float, B, kFma, kStages>(p, it.strip, it.blk, ring, bars, load_base);
+    ok = warp_item2d<S, float, B, kFma, kStages>(p, strip, blk, ring, bars, load_base);
   }
   __syncwarp();  // the slot is rewritten by the next item
-  return ok;
+  return ok ? load_base : ~0u;
 }
 
 template <class S>
 __device__ __forceinline__ bool dispatch_b(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
                                            unsigned &load_base, int *err, unsigned char *slot) {
   constexpr int BS = batch_degree<S>();
-  if (it.b == BS) return run_item<S, BS>(g, it, ring, bars, load_base, err, slot);
+  unsigned next = ~0u;
+  if (it.b == BS) next = run_item<S, BS>(&g, it.k, it.strip, it.blk, ring, bars, load_base, err, slot);
   if constexpr (BS != 1) {
-    if (it.b == 1) return run_item<S, 1>(g, it, ring, bars, load_base, err, slot);
+    if (it.b == 1) next = run_item<S, 1>(&g, it.k, it.strip, it.blk, ring, bars, load_base, err, slot);
   }
-  return false;
+  if (next == ~0u) return false;
+  load_base = next;
+  return true;
 }
 
 __device__ __forceinline__ bool dispatch(const GridDev &g, const Item &it, float *ring, uint64_t *bars,
@@ -158,26 +178,26 @@ __device__ __forceinline__ bool dispatch(const GridDev &g, const Item &it, float
   }
 }
 
-__global__ void __launch_bounds__(kWpc * 32, 3) batch2d_kernel(const __grid_constant__ Args a) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  float *ring;
-  uint64_t *bars;
-  warp_ring2d<float, kWpc, kStages>(smem_raw, ring, bars);
+// One work item on one warp: wait (bounded) until the stream blocks it
+// reads have finished the grid's earlier time blocks, run it, count it done.
+// False when a wait gave up (the error word says which).
+__device__ __forceinline__ bool persistent_item(const Args &a, unsigned idx, float *ring, uint64_t *bars,
+                                                unsigned &load_base, unsigned char *slot) {
   const int lane = threadIdx.x & 31;
-  unsigned char *slot = smem_raw + (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t)) +
-                        (size_t)(threadIdx.x >> 5) * kParamSlot;
-  unsigned load_base = 0;
-  while (true) {
-    unsigned idx = 0;
-    if (lane == 0) idx = atomicAdd(a.next, 1u);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= (unsigned)a.nitems) break;
-    const Item it = a.items[idx];
-    bool ok = true;
-    if (lane == 0 && it.need > 0) {
-      const unsigned long long t0 = global_ns();
+  const Item it = a.items[idx];
+  bool ok = true;
+  const GridDev &g = a.grids[it.grid];
+  // the counter this item completes, and the ones it waits on: the stream
+  // blocks it reads (b*r rows at most past its own, less than one block)
+  // and whose readers its writes must follow
+  const int cown = g.cbase + (g.ccount > 1 ? it.blk : 0);
+  if (lane == 0 && it.need > 0) {
+    const unsigned long long t0 = global_ns();
+    const int lo = g.ccount > 1 ? max(0, it.blk - 1) : 0;
+    const int hi = g.ccount > 1 ? min(g.ccount - 1, it.blk + 1) : 0;
+    for (int c = lo; c <= hi && ok; ++c) {
       unsigned spins = 0;
-      while (ld_acquire(&a.done[it.grid]) < (unsigned)it.need) {
+      while (ld_acquire(&a.done[g.cbase + c]) < (unsigned)it.need) {
         if (++spins > 64) {
           __nanosleep(200);
           if (global_ns() - t0 > kWaitLimitNs) {
@@ -187,23 +207,58 @@ __global__ void __launch_bounds__(kWpc * 32, 3) batch2d_kernel(const __grid_cons
           }
         }
       }
-      asm volatile("fence.proxy.async.global;" ::: "memory");
     }
-    if (!__all_sync(0xffffffffu, ok)) break;
-    __syncwarp();
-    if (!dispatch(a.grids[it.grid], it, ring, bars, load_base, a.err, slot)) {
-      if (lane == 0) atomicOr(a.err, ERR_WAIT_TIMEOUT);
-      break;
-    }
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) atomicAdd(&a.done[it.grid], 1u);
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  if (!__all_sync(0xffffffffu, ok)) return false;
+  __syncwarp();
+  if (!dispatch(g, it, ring, bars, load_base, a.err, slot)) {
+    if (lane == 0) atomicOr(a.err, ERR_WAIT_TIMEOUT);
+    return false;
+  }
+  __threadfence();
+  __syncwarp();
+  if (lane == 0) atomicAdd(&a.done[cown], 1u);
+  return true;
+}
+
+// Persistent: each CTA takes groups of kWpc consecutive items from an
+// atomic counter, warp w running item group * kWpc + w, the way the layered
+// schedule's CTAs run consecutive items. Neighbouring items are the same
+// stencil and degree (consecutive strips of one stream block), so the CTAs
+// resident on an SM mostly run one kernel variant and share its code in the
+// instruction cache; warps that took items one at a time mixed variants on
+// every SM and stalled on instruction fetch. Groups are taken in order and
+// an item waits only on earlier items, whose groups were taken by running
+// CTAs: progress does not need every CTA resident.
+__global__ void __launch_bounds__(kWpc * 32, kPersistentCtas) batch2d_kernel(const __grid_constant__ Args a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ unsigned s_group;
+  __shared__ int s_stop;
+  float *ring;
+  uint64_t *bars;
+  warp_ring2d<float, kWpc, kStages>(smem_raw, ring, bars);
+  unsigned char *slot = smem_raw + (size_t)kWpc * kStages * (128 * sizeof(float) + sizeof(uint64_t)) +
+                        (size_t)(threadIdx.x >> 5) * kParamSlot;
+  unsigned load_base = 0;
+  if (threadIdx.x == 0) s_stop = 0;
+  while (true) {
+    if (threadIdx.x == 0) s_group = atomicAdd(a.next, 1u);
+    __syncthreads();
+    const unsigned first = s_group * (unsigned)kWpc;
+    const bool stop = s_stop != 0 || first >= (unsigned)a.nitems;
+    __syncthreads();  // s_group and s_stop are read before they are written again
+    if (stop) break;
+    const unsigned idx = first + (threadIdx.x >> 5);
+    if (idx < (unsigned)a.nitems && !persistent_item(a, idx, ring, bars, load_base, slot) &&
+        (threadIdx.x & 31) == 0)
+      s_stop = 1;
   }
 }
 
 // One time block of every grid: warp w runs item first + w. Kernel
 // boundaries order the blocks, so nothing here waits.
-__global__ void __launch_bounds__(kWpc * 32, 3) batch_layer_kernel(const __grid_constant__ Args a, int first,
+__global__ void __launch_bounds__(kWpc * 32, kLayerCtas) batch_layer_kernel(const __grid_constant__ Args a, int first,
                                                                    int count) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const long long gw = (long long)blockIdx.x * kWpc + (threadIdx.x >> 5);
@@ -258,7 +313,8 @@ using namespace gbs;
 struct gbs_batch {
   gbs::batchdetail::GridDev *d_grids = nullptr;
   gbs::batchdetail::Item *d_items = nullptr;
-  unsigned *d_counters = nullptr;  // [0] next, [1..] done per grid
+  unsigned *d_counters = nullptr;  // [0] next, [1..] done per stream block of every grid
+  int ncounters = 0;
   int ngrids = 0, nitems = 0, ctas = 0;
   long long cells = 0;             // sum over grids of interior cells * timestep
   size_t smem = 0;
@@ -334,12 +390,21 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
       if (st != GBS_OK) return st;
     }
   }
+  // one completion counter per stream block of every grid
+  int ncounters = 0;
+  for (int g = 0; g < ngrids; ++g) {
+    gd[g].cbase = ncounters;
+    gd[g].ccount = gd[g].nblocks;
+    ncounters += gd[g].nblocks;
+  }
   // Items ordered by time block, then stencil, then grid: every grid's
   // blocks stay in order (each item's dependencies come earlier in the
   // list), all grids advance together (the critical path is the longest
   // grid's chain of blocks, not a sum over groups), and warps taking
   // neighbouring items run the same kernel variant (one instruction-cache
-  // working set).
+  // working set). An item waits until its stream block and the two beside
+  // it have finished every earlier time block: `need` counts the items of
+  // one stream block in the grid's earlier time blocks.
   std::vector<Item> items;
   std::vector<int> done_before(ngrids, 0);
   size_t kmax = 0;
@@ -358,18 +423,19 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
       const int need = done_before[g];
       for (int blk = 0; blk < gd[g].nblocks; ++blk)
         for (int st = 0; st < nstrips; ++st) items.push_back(Item{g, (int)k, b, st, blk, need, 0, 0});
-      done_before[g] += nstrips * gd[g].nblocks;
+      done_before[g] += nstrips;
     }
   }
   auto *h = new gbs_batch();
   h->ngrids = ngrids;
+  h->ncounters = ncounters;
   h->nitems = (int)items.size();
   h->cells = cells;
   for (auto &b : blocks) h->launches_plain += (int)b.size();
   cudaError_t e;
   if ((e = cudaMalloc(&h->d_grids, sizeof(GridDev) * ngrids)) != cudaSuccess ||
       (e = cudaMalloc(&h->d_items, sizeof(Item) * std::max<size_t>(1, items.size()))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_counters, sizeof(unsigned) * (ngrids + 1))) != cudaSuccess) {
+      (e = cudaMalloc(&h->d_counters, sizeof(unsigned) * (ncounters + 1))) != cudaSuccess) {
     gbs_batch_destroy(h);
     return cuda_fail(e, "batch: cudaMalloc");
   }
@@ -417,7 +483,7 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
         ++h->kernels;
       }
     } else {
-      cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned) * (ngrids + 1), cs);
+      cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned) * (ncounters + 1), cs);
       batch2d_kernel<<<h->ctas, kWpc * 32, h->smem, cs>>>(a);
       h->kernels = 1;
     }
@@ -473,6 +539,15 @@ void split_blocks(int T, int bs, int &full, int &single) {
 
 gbs_status run(const gbs_batch_grid *grids, int ngrids, cudaStream_t stream) {
   if (!grids || ngrids <= 0) return fail(GBS_ERR_INVALID, "batch (no allocation): no grids");
+  {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) {
+      (void)cudaGetLastError();
+      cap = cudaStreamCaptureStatusNone;
+    }
+    if (cap != cudaStreamCaptureStatusNone)
+      return fail(GBS_ERR_INVALID, "batch (no allocation): the call synchronises its stream and cannot be captured");
+  }
   if (ngrids > kMaxGrids)
     return fail(GBS_ERR_INVALID, "batch (no allocation): %d grids, at most %d fit its static scratch", ngrids,
                 kMaxGrids);
@@ -508,6 +583,8 @@ gbs_status run(const gbs_batch_grid *grids, int ngrids, cudaStream_t stream) {
     const int ni = L.dims[0] - 2 * s->rad;
     x.sl = std::min(ni, 128);
     x.nblocks = (ni + x.sl - 1) / x.sl;
+    x.cbase = g;  // one counter per grid: the scratch holds ngrids + 1
+    x.ccount = 1;
     const double div = bg.divisor != 0.0 ? bg.divisor : (double)s->divisor;
     const bool fold = kFma && s->divisor;
     const int nt = s->kind == 1 ? 1 : s->nterms;

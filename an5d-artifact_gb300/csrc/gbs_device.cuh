@@ -31,6 +31,11 @@ constexpr unsigned long long kWaitLimitNs = 1000ull * 1000ull * 1000ull;
 
 template <int N> using IC = std::integral_constant<int, N>;
 
+// Forces a lambda inline. A lambda the compiler keeps as a call (it did so
+// for the row loop of a kernel variant inside the batched dispatcher) has
+// its captured locals, the register windows among them, in local memory.
+#define GBS_INL __attribute__((always_inline))
+
 // Compile-time loop: f(IC<0>), ..., f(IC<N-1>).
 template <int N, class F, int... Is>
 __device__ __forceinline__ void static_for_impl(F &&f, std::integer_sequence<int, Is...>) {

@@ -312,7 +312,7 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
 
   // One pipeline step at row pp with phase PH. CAREFUL steps handle the
   // stream ends, halo rows and edge columns; the others assume none occur.
-  auto step = [&](auto PHI, auto CAREI, int pp) {
+  auto step = [&](auto PHI, auto CAREI, int pp) GBS_INL {
     constexpr int ph = decltype(PHI)::value;
     constexpr bool careful = decltype(CAREI)::value;
     T x[V];
@@ -374,7 +374,7 @@ __device__ __forceinline__ bool warp_item2d(const Params2D<T, ST::kTerms> &p, in
   };
 
   // steps [lo, hi) in whole groups of NPH phases, starting at a group boundary
-  auto run = [&](int lo, int hi, auto CAREI) {
+  auto run = [&](int lo, int hi, auto CAREI) GBS_INL {
 #pragma unroll 1
     for (int pb = lo; pb < hi && ok; pb += NPH) {
       static_for<NPH>([&](auto PHI) {

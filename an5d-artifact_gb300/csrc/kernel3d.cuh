@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(TJ * 32, gbs_min_ctas(TJ * 32))
   }
   __syncthreads();
 
-  auto issue = [&](int plane) {  // lane 0 of every warp: this warp's row of `plane`
+  auto issue = [&](int plane) GBS_INL {  // lane 0 of every warp: this warp's row of `plane`
     const int n = plane - pstart;
     const int s = n % NS;
     T *dstp = ring0 + (size_t)s * PLANE + (size_t)(w + R) * ROW;
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(TJ * 32, gbs_min_ctas(TJ * 32))
 
   // waits (bounded) for level-0 plane pl; the give-up decision is CTA-uniform
   // and the call is the step's barrier
-  auto wait_plane = [&](int pl) -> bool {
+  auto wait_plane = [&](int pl) GBS_INL -> bool {
     bool got = true;
     if (pl < pend) {
       const int n = pl - pstart;

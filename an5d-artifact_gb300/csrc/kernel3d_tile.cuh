@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
 
   // thread 0: the whole box of level-0 plane `plane` into its stage
   int issued = pstart;  // thread 0: one past the last plane issued
-  auto issue = [&](int plane) {
+  auto issue = [&](int plane) GBS_INL {
     const int st = (plane - pstart) % NS;
     mbar_arrive_expect_tx(&bars[st], (unsigned)G::BOX_BYTES);
     tma_load_3d(ring0 + (size_t)st * PLANE, &p.tmap, ws - PADE, jt - R, plane, &bars[st]);
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
 
   bool ok = true;
   int waited = pstart;
-  auto wait_plane = [&](int pl) -> bool {
+  auto wait_plane = [&](int pl) GBS_INL -> bool {
     bool got = true;
     if (pl < pend) {
       const int n = pl - pstart;
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
     return true;
   };
   // loads the fixed halo values level l needs at step s (output plane q)
-  auto fetch_carry = [&](auto LI, int s) {
+  auto fetch_carry = [&](auto LI, int s) GBS_INL {
     constexpr int l = decltype(LI)::value;
     const int q = s - l * (R + 1) - R;
     const bool need = (q >= 0 && q < p.d0) && (q < R || q >= p.d0 - R || warp_jhalo || kedge);
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(NW * 32, gbs_min_ctas(NW * 32))
     }
   };
 
-  auto step = [&](auto PHI, int s) {
+  auto step = [&](auto PHI, int s) GBS_INL {
     constexpr int ph = decltype(PHI)::value;
     if (threadIdx.x == 0 && s > pstart) {
       const int pf = s - 1 + NS;  // the stage of plane s-1 is free since the last barrier
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, gbs_min_ctas((NW + 1) * 32))
   });
 
   bool ok = true;
-  auto step = [&](auto PHI, int s) {
+  auto step = [&](auto PHI, int s) GBS_INL {
     constexpr int ph = decltype(PHI)::value;
     const int n = s - pstart;
     const int st = n % NS;

@@ -11,9 +11,9 @@ A step is one full time loop (T timesteps) over each grid of the workload:
 * batched: 512 independent fp32 2-D grids, sides log-uniform in [128, 4096]
   per axis, stencil uniform over star2d1r-4r, box2d1r-4r, j2d5pt, j2d9pt,
   T uniform in [16, 512], normalised random coefficients per grid, all
-  advanced by ONE CUDA-graph launch (--batch-mode: streams, the default,
-  persistent or layered); the line also reports the same work done by
-  per-grid plain launches, one grid after another.
+  advanced by ONE CUDA-graph launch (--batch-mode: layered, the default and
+  the fastest, persistent or streams); the line also reports the same work
+  done by per-grid plain launches, one grid after another.
 * adjoint: the gradient of the time loop (gbs_adjoint_forward/backward):
   j2d5pt f32 2048^2 T=1024 (checkpoints every 32, gradients of u_0 and the
   coefficients), gradient2d f64 4096^2 T=512, j3d27pt f32 384^3 T=256 and
@@ -780,7 +780,7 @@ def main(argv=None):
     ap.add_argument("--bs1", type=int, default=0, help="3-D tile rows of every grid (0: the tuned shape)")
     ap.add_argument("--batch-grids", type=int, default=512, help="batched workload: number of grids")
     ap.add_argument("--batch-tmax", type=int, default=512, help="batched workload: largest T")
-    ap.add_argument("--batch-mode", default="streams", choices=["persistent", "layered", "streams"],
+    ap.add_argument("--batch-mode", default="layered", choices=["persistent", "layered", "streams"],
                     help="batched workload: scheduling of the work items")
     ap.add_argument("--e2e-steps", type=int, default=3, help="timed host-buffer samples (at most --steps)")
     ap.add_argument("--no-check", action="store_true", help="skip the per-grid error check against the oracle")

@@ -238,9 +238,10 @@ void gbs_batch_destroy(gbs_batch *plan);
  * 1 MB each), which every GPU that loads the library holds until the process
  * exits; host staging uses static host arrays. Batches of more than
  * GBS_NOALLOC_MAX_GRIDS grids or GBS_NOALLOC_MAX_ITEMS work items are
- * rejected with GBS_ERR_INVALID. The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture. Every call reuses the same array (its counters and
+ * rejected with GBS_ERR_INVALID. A call copies its tables in and waits for
+ * the kernel on `stream`, so it cannot be part of a stream capture: on a
+ * capturing stream it returns GBS_ERR_INVALID and does nothing. Every call
+ * reuses the same array (its counters and
  * error word are cleared on each call), so calls that overlap on the GPU
  * race; calls from one process are serialised, and each call returns after
  * its work has finished on `stream`, reporting device-side timeouts as

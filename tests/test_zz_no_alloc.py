@@ -93,3 +93,25 @@ def test_no_alloc_rejects_oversized_batches():
         capi.batch_run_noalloc([(big, 512, None)])  # about 155k work items
     assert e.value.status == capi.GBS_ERR_INVALID
     assert "work items" in capi.lib().gbs_last_error().decode()
+
+
+def test_no_alloc_refuses_a_capturing_stream():
+    """The call copies its tables in and waits on its stream, so it cannot be
+    captured: on a capturing stream it returns GBS_ERR_INVALID and issues
+    nothing, and the capture stays valid."""
+    g = DeviceGrid("star2d1r", np.float32, [8, 8])
+    x = torch.zeros(4, device="cuda")
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    status = None
+    with torch.cuda.graph(graph, stream=s):
+        x.add_(1.0)
+        try:
+            capi.batch_run_noalloc([(g, 1, None)], stream=s.cuda_stream)
+        except capi.GbsError as e:
+            status = e.status
+    assert status == capi.GBS_ERR_INVALID
+    assert "captured" in capi.lib().gbs_last_error().decode()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(x, torch.ones(4, device="cuda"))
