@@ -579,6 +579,7 @@ def run_adjoint(args, rank, world):
     cases, tot_cells, tot_bwd, tot_e2e, h2d, d2h, launches = [], 0, 0.0, 0.0, 0, 0, 0
     gen = torch.Generator(device=dev)
     todo = list(ADJOINT_CASES)
+    clk = ClockSampler(dev.index).__enter__()  # clocks over every timed run below
     if args.only:  # e.g. j2d5pt:float32 (small profiling cases)
         keep = {tuple(x.split(":")) for x in args.only.split(",")}
         todo = [c for c in todo if (c[0], np.dtype(c[1]).name) in keep][:1]
@@ -715,6 +716,7 @@ def run_adjoint(args, rank, world):
                  "one_at_a_time_backward_ms": round(sum_b, 3),
                  "backward_speedup": round(sum_b / statistics.median(bw), 3)}
         torch.cuda.empty_cache()
+    clk.__exit__(None, None, None)
     tot_bwd = max_over_ranks(tot_bwd, world, dev)
     value = tot_cells * world / (tot_bwd * 1e-3) / 1e9
     hbm, peak_kind = load_peaks()
@@ -743,6 +745,7 @@ def run_adjoint(args, rank, world):
                      "frac": round(achieved / hbm, 4), "traffic": None,
                      "kernel": f"backward of {dom['stencil']} {dom['dtype']} {'x'.join(map(str, dom['n']))}",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "clocks": clk.summary(),
         "gpu_launches": launches,
     }
 
