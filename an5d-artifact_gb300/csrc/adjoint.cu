@@ -266,22 +266,33 @@ __device__ __forceinline__ void load_edges(RowEdges<T, V, R> &ed, const T *p, lo
     if (lane >= 32 - dl) ed.right[x - V] = p[rowbase + x];
   });
 }
-// Element x (relative to the lane's first column, x in [-R, V+R)) of row
-// offset D of the lane's 2R+1-row window: from its own vector, from a lane up
-// to R/V away, or, for the lanes whose source lane lies outside the warp,
-// from the row's cached edges
-template <int V, int R, int D, int X, typename T>
-__device__ __forceinline__ T row_value_cached(const T (&rows)[2 * R + 1][V], const RowEdges<T, V, R> (&ed)[2 * R + 1],
+// Element x (relative to the lane's first column, x in [-R, V+R)) of the row
+// at window position P: from the lane's own vector, from a lane up to R/V
+// away, or, for the lanes whose source lane lies outside the warp, from the
+// row's cached edges
+template <int V, int R, int P, int X, typename T, int NWIN>
+__device__ __forceinline__ T row_value_cached(const T (&rows)[NWIN][V], const RowEdges<T, V, R> (&ed)[NWIN],
                                               int lane) {
-  T v = row_elem<V, X>(rows[D + R]);
+  T v = row_elem<V, X>(rows[P]);
   if constexpr (X < 0) {
     constexpr int dl = (-X + V - 1) / V;
-    if (lane < dl) v = ed[D + R].left[X + R];
+    if (lane < dl) v = ed[P].left[X + R];
   } else if constexpr (X >= V) {
     constexpr int dl = X / V;
-    if (lane >= 32 - dl) v = ed[D + R].right[X - V];
+    if (lane >= 32 - dl) v = ed[P].right[X - V];
   }
   return v;
+}
+
+// rows of lam (and u) the adjoint step loads per batch: one memory latency
+// per batch of output rows instead of one per row. The window holds 2R + K
+// rows of each array, so the batch shrinks with the radius and for double
+// (radius 1 float at K = 4 takes 116 registers with the coefficient
+// products; larger windows spill).
+template <typename T, int R>
+constexpr int adj_batch() {
+  if (sizeof(T) == 4) return R == 1 ? 4 : (R == 2 ? 2 : 1);
+  return R == 1 ? 2 : 1;
 }
 
 // 2-D linear adjoint step, fused: lam_out(y) = sum_k c_k/d lam(y - o_k) on
@@ -293,8 +304,10 @@ __device__ __forceinline__ T row_value_cached(const T (&rows)[2 * R + 1][V], con
 // that a step is bound by kernel latency. The first `interior_blocks` CTAs
 // take work units of one 32*V-column segment by `rows` interior rows: each
 // lane streams its aligned 16-byte vector of V columns down the rows,
-// keeping the 2R+1 rows of lam (and of u) that the current output row
-// needs in registers, so that every row is loaded once per unit; in-row
+// keeping the rows of lam (and of u) that the next batch of output rows
+// needs in registers, so that every row is loaded once per unit and the
+// loads of a batch of rows are in flight together (a unit of a few rows per
+// warp is otherwise a chain of dependent memory latencies); in-row
 // neighbours come from the lanes up to R/V away (the warp's edge lanes load
 // theirs). The CTAs after them take the halo cells (one thread each).
 template <class ST, typename T, bool WANT_COEF>
@@ -333,68 +346,83 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
     const int c0 = R + seg * SEG + lane * V;        // the lane's first column; 16-byte aligned
     const int nvalid = min(V, g.last - R - c0);     // columns of the group inside the interior
     const long long col = (long long)g.shift + c0;
-    // windows of rows i-R .. i+R (position d+R holds row i+d)
-    T lw[W][V], uw[W][V];
-    RowEdges<T, V, R> le[W], ue[W];  // the segment-end elements of each window row
-    static_for<W - 1>([&](auto DI) {
-      constexpr int d = decltype(DI)::value - R;  // rows ia-R .. ia+R-1
-      const long long rb = (long long)(ia + d) * g.pitch + col;
-      ld_vec<T, V>(lw[d + R + 1], lam + rb);
-      load_edges<T, V, R>(le[d + R + 1], lam, rb, lane);
+    // windows of rows i-R .. i+R+K-1 (position p holds row i-R+p), refilled
+    // K rows at a time: the K new rows of lam (and u) are loaded together
+    constexpr int K = adj_batch<T, R>();
+    constexpr int NWIN = 2 * R + K;
+    T lw[NWIN][V], uw[WANT_COEF ? NWIN : 1][V];
+    RowEdges<T, V, R> le[NWIN], ue[WANT_COEF ? NWIN : 1];  // the segment-end elements of each row
+    static_for<2 * R>([&](auto PI) {
+      constexpr int pp = decltype(PI)::value;  // rows ia-R .. ia+R-1
+      const long long rb = (long long)(ia - R + pp) * g.pitch + col;
+      ld_vec<T, V>(lw[pp], lam + rb);
+      load_edges<T, V, R>(le[pp], lam, rb, lane);
       if constexpr (WANT_COEF) {
-        ld_vec<T, V>(uw[d + R + 1], u + rb);
-        load_edges<T, V, R>(ue[d + R + 1], u, rb, lane);
+        ld_vec<T, V>(uw[pp], u + rb);
+        load_edges<T, V, R>(ue[pp], u, rb, lane);
       }
     });
 #pragma unroll 1
-    for (int i = ia; i < ib; ++i) {
-      // slide: drop row i-R-1, load row i+R
-      static_for<W - 1>([&](auto DI) {
-        constexpr int d = decltype(DI)::value;
+    for (int i = ia; i < ib; i += K) {
+      // load rows i+R .. i+R+K-1 (those below ib+R; the rest are not read)
+      static_for<K>([&](auto KI) {
+        constexpr int kk = decltype(KI)::value;
+        if (i + kk < ib) {
+          const long long rb = (long long)(i + R + kk) * g.pitch + col;
+          ld_vec<T, V>(lw[2 * R + kk], lam + rb);
+          load_edges<T, V, R>(le[2 * R + kk], lam, rb, lane);
+          if constexpr (WANT_COEF) {
+            ld_vec<T, V>(uw[2 * R + kk], u + rb);
+            load_edges<T, V, R>(ue[2 * R + kk], u, rb, lane);
+          }
+        }
+      });
+      static_for<K>([&](auto KI) {
+        constexpr int kk = decltype(KI)::value;  // output row i+kk: window positions kk .. kk+2R
+        if (i + kk < ib) {
+          const long long base = (long long)(i + kk) * g.pitch + col;
+          T sv[V];
+#pragma unroll
+          for (int e = 0; e < V; ++e) sv[e] = T(0);
+          static_for<NT>([&](auto TI) {
+            constexpr int t = decltype(TI)::value;
+            constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+            static_for<V>([&](auto EI) {
+              constexpr int e = decltype(EI)::value;
+              sv[e] = fma(cf.c[t], row_value_cached<V, R, kk + R - di, e - dj>(lw, le, lane), sv[e]);
+            });
+          });
+          if constexpr (WANT_COEF) {
+            static_for<NT>([&](auto TI) {
+              constexpr int t = decltype(TI)::value;
+              constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
+              static_for<V>([&](auto EI) {
+                constexpr int e = decltype(EI)::value;
+                const T uv = row_value_cached<V, R, kk + R + di, e + dj>(uw, ue, lane);
+                if (e < nvalid) acc[t] = fma(lw[kk + R][e], uv, acc[t]);
+              });
+            });
+          }
+          if (nvalid == V) {
+            st_vec<T, V>(lam_out + base, sv);
+          } else {
+#pragma unroll
+            for (int e = 0; e < V; ++e)
+              if (e < nvalid) lam_out[base + e] = sv[e];
+          }
+        }
+      });
+      // slide by K: rows i+K-R .. i+K+R-1 to positions 0 .. 2R-1
+      static_for<2 * R>([&](auto PI) {
+        constexpr int pp = decltype(PI)::value;
 #pragma unroll
         for (int e = 0; e < V; ++e) {
-          lw[d][e] = lw[d + 1][e];
-          if constexpr (WANT_COEF) uw[d][e] = uw[d + 1][e];
+          lw[pp][e] = lw[pp + K][e];
+          if constexpr (WANT_COEF) uw[pp][e] = uw[pp + K][e];
         }
-        le[d] = le[d + 1];
-        if constexpr (WANT_COEF) ue[d] = ue[d + 1];
+        le[pp] = le[pp + K];
+        if constexpr (WANT_COEF) ue[pp] = ue[pp + K];
       });
-      const long long base = (long long)i * g.pitch + col;
-      ld_vec<T, V>(lw[W - 1], lam + base + (long long)R * g.pitch);
-      load_edges<T, V, R>(le[W - 1], lam, base + (long long)R * g.pitch, lane);
-      if constexpr (WANT_COEF) {
-        ld_vec<T, V>(uw[W - 1], u + base + (long long)R * g.pitch);
-        load_edges<T, V, R>(ue[W - 1], u, base + (long long)R * g.pitch, lane);
-      }
-      T sv[V];
-#pragma unroll
-      for (int e = 0; e < V; ++e) sv[e] = T(0);
-      static_for<NT>([&](auto TI) {
-        constexpr int t = decltype(TI)::value;
-        constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-        static_for<V>([&](auto EI) {
-          constexpr int e = decltype(EI)::value;
-          sv[e] = fma(cf.c[t], row_value_cached<V, R, -di, e - dj>(lw, le, lane), sv[e]);
-        });
-      });
-      if constexpr (WANT_COEF) {
-        static_for<NT>([&](auto TI) {
-          constexpr int t = decltype(TI)::value;
-          constexpr int di = ST::kOff[t][0], dj = ST::kOff[t][1];
-          static_for<V>([&](auto EI) {
-            constexpr int e = decltype(EI)::value;
-            const T uv = row_value_cached<V, R, di, e + dj>(uw, ue, lane);
-            if (e < nvalid) acc[t] = fma(lw[R][e], uv, acc[t]);
-          });
-        });
-      }
-      if (nvalid == V) {
-        st_vec<T, V>(lam_out + base, sv);
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e)
-          if (e < nvalid) lam_out[base + e] = sv[e];
-      }
     }
   }
   if constexpr (WANT_COEF) {
