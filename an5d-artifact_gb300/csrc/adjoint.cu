@@ -39,6 +39,7 @@
 
 #include <algorithm>
 #include <functional>
+#include <map>
 #include <mutex>
 #include <cstring>
 #include <vector>
@@ -701,20 +702,24 @@ int one_wave(K kernel) {
   return std::max(1, std::min(kCoefBlocks, nb * sms));
 }
 
-// one_wave(kernel) for the current device, computed once per device ordinal
-// (a process may drive GPUs with different SM counts)
+// one_wave(kernel) on the current device, computed once per (device
+// ordinal, kernel): kernels of the same signature (the variants with and
+// without products, stencils with as many terms) differ in registers and so
+// in resident CTAs, and a process may drive GPUs with different SM counts
 template <class K>
 int wave_cached(K kernel) {
   static std::mutex mu;
-  static int cache[64] = {};
+  static std::map<std::pair<int, const void *>, int> cache;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+  if (cudaGetDevice(&dev) != cudaSuccess) {
     (void)cudaGetLastError();
     return one_wave(kernel);
   }
   std::lock_guard<std::mutex> lk(mu);
-  if (cache[dev] == 0) cache[dev] = one_wave(kernel);
-  return cache[dev];
+  const auto key = std::make_pair(dev, reinterpret_cast<const void *>(kernel));
+  auto it = cache.find(key);
+  if (it == cache.end()) it = cache.emplace(key, one_wave(kernel)).first;
+  return it->second;
 }
 
 // one thread per halo cell of the interior rows, one warp per segment of an all-halo row
