@@ -324,6 +324,7 @@ struct gbs_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int launches_plain = 0;          // what per-grid plain launches would need
+  long long hbm_bytes = 0;         // algorithmic: each fused launch reads and writes the interior once
   int mode = 0, kernels = 0;
 };
 
@@ -437,6 +438,8 @@ extern "C++" gbs_status GBS_BATCH_FN(gbs_batch_build)(const gbs_batch_grid *grid
   h->nitems = (int)items.size();
   h->cells = cells;
   for (auto &b : blocks) h->launches_plain += (int)b.size();
+  for (int g = 0; g < ngrids; ++g)
+    h->hbm_bytes += 2LL * (long long)blocks[g].size() * grids[g].n[0] * grids[g].n[1] * (long long)sizeof(float);
   cudaError_t e;
   if ((e = cudaMalloc(&h->d_grids, sizeof(GridDev) * ngrids)) != cudaSuccess ||
       (e = cudaMalloc(&h->d_items, sizeof(Item) * std::max<size_t>(1, items.size()))) != cudaSuccess ||
@@ -721,7 +724,7 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int dtype, int
   const int nbr = branches();
   std::vector<gbs_desc> ds(ngrids);
   std::vector<double> work(ngrids);
-  long long cells = 0;
+  long long cells = 0, hbm = 0;
   int launches = 0;
   for (int g = 0; g < ngrids; ++g) {
     const gbs_batch_grid &bg = grids[g];
@@ -761,6 +764,7 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int dtype, int
     launches += pi.launches;
     const long long area = (long long)d.n[0] * d.n[1] * (s->dim == 3 ? d.n[2] : 1);
     cells += area * bg.timestep;
+    hbm += 2LL * pi.launches * area * (dtype == GBS_F64 ? 8 : 4);
     work[g] = (double)area * bg.timestep;
   }
   int *err = nullptr;
@@ -773,6 +777,7 @@ gbs_status build_streams(const gbs_batch_grid *grids, int ngrids, int dtype, int
   h->ngrids = ngrids;
   h->cells = cells;
   h->launches_plain = launches;
+  h->hbm_bytes = hbm;
   h->mode = GBS_BATCH_STREAMS;
   cudaStream_t cs = nullptr, side[kMaxStreams] = {};
   cudaEvent_t fork = nullptr, join[kMaxStreams] = {};
@@ -865,6 +870,7 @@ gbs_status gbs_batch_info(const gbs_batch *plan, gbs_batch_stats *out) {
   out->plain_launches = h->launches_plain;
   out->kernels = h->kernels;
   out->mode = h->mode;
+  out->hbm_bytes = h->hbm_bytes;
   return GBS_OK;
 }
 

@@ -61,7 +61,7 @@ class BatchGrid(ctypes.Structure):
 class BatchStats(ctypes.Structure):
     _fields_ = [("grids", ctypes.c_int), ("items", ctypes.c_int), ("ctas", ctypes.c_int),
                 ("plain_launches", ctypes.c_int), ("cell_updates", ctypes.c_longlong),
-                ("kernels", ctypes.c_int), ("mode", ctypes.c_int)]
+                ("kernels", ctypes.c_int), ("mode", ctypes.c_int), ("hbm_bytes", ctypes.c_longlong)]
 
 
 _lib = None

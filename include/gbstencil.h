@@ -196,13 +196,16 @@ typedef struct gbs_batch_stats {
   long long cell_updates;  /* sum of n[0]*n[1]*timestep */
   int kernels;             /* kernel nodes in the plan's graph */
   int mode;                /* GBS_BATCH_PERSISTENT | GBS_BATCH_LAYERED | GBS_BATCH_STREAMS */
+  long long hbm_bytes;     /* algorithmic HBM bytes of one run: each fused launch (time block)
+                              of a grid reads and writes its interior once */
 } gbs_batch_stats;
 
 /* How a batch plan schedules its work:
  * GBS_BATCH_PERSISTENT: one persistent kernel over work items (grid, time
- *   block, strip, stream block) of 2-D float grids; warps take items in
- *   time-block order from an atomic counter and wait (bounded) on per-grid
- *   completion counters for the grid's previous time block.
+ *   block, strip, stream block) of 2-D float grids; CTAs take groups of
+ *   consecutive items in time-block order from an atomic counter, and an
+ *   item waits (bounded) until its stream block and the two beside it have
+ *   finished the grid's earlier time blocks (per-block completion counters).
  * GBS_BATCH_LAYERED: the same 2-D work items, one kernel node per time block
  *   in the graph, each over every grid's items of that block; kernel
  *   boundaries order the blocks, so nothing waits on the device.

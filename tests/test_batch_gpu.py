@@ -49,6 +49,11 @@ def test_batch_matches_oracle(mode, sched):
     b = capi.Batch(entries, fp_mode=mode, mode=sched)
     st = b.stats()
     assert st.grids == len(specs)
+    # algorithmic HBM bytes: every time block of a grid reads and writes its
+    # interior once, so between one pass per step and one pass per run
+    upd = sum(int(np.prod(n)) * T for name, n, T in specs)
+    assert st.cell_updates == upd
+    assert sum(8 * int(np.prod(n)) for name, n, T in specs if T > 0) <= st.hbm_bytes <= 8 * upd
     s = torch.cuda.current_stream()
     b.run(s.cuda_stream)
     capi.sync(s.cuda_stream)
