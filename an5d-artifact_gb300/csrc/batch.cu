@@ -5,17 +5,21 @@
 // Work items are (grid, time block, strip, stream block): one warp runs the
 // same temporally-blocked pipeline as the single-grid kernel
 // (warp_item2d) on one item. The host orders the items by time block;
-// persistent warps take them in that order from an atomic counter. An item
-// of time block k of grid g starts once every item of g's earlier blocks has
-// finished (a per-grid completion counter reaching the item's `need`). The
-// order (by time block) makes this deadlock-free: every item an item waits
-// on was taken earlier by a running warp that never waits on a later item.
-// Waits are bounded (the error word is set and the warp stops).
+// persistent CTAs take groups of consecutive items in that order from an
+// atomic counter. An item of time block k of grid g starts once its stream
+// block and the two beside it have finished g's earlier blocks (completion
+// counters per stream block, or one per grid in the run without
+// allocation, reaching the item's `need`). The order (by time block) makes
+// this deadlock-free: every item an item waits on was taken earlier by a
+// running CTA that never waits on a later item. Waits are bounded (the
+// error word is set and the CTA stops). The layered schedule runs the same
+// items as one kernel node per time block instead, with no waits.
 //
 // Memory ordering: a finishing item's lanes fence their stores, then lane 0
-// increments the grid's counter; a starting item's lane 0 reads the counter
-// with acquire semantics and issues a proxy fence before its bulk copies (an
-// async-proxy read) touch the data. Loads outside the bulk copies bypass L1.
+// increments its block's counter; a starting item's lane 0 reads the
+// counters with acquire semantics and issues a proxy fence before its bulk
+// copies (an async-proxy read) touch the data. Loads outside the bulk copies
+// bypass L1.
 //
 // Built twice: -DGBS_FMA=0 (exact mode) and -DGBS_FMA=1.
 #include <cuda_runtime.h>

@@ -218,7 +218,7 @@ typedef struct gbs_batch_stats {
 enum { GBS_BATCH_PERSISTENT = 0, GBS_BATCH_LAYERED = 1, GBS_BATCH_STREAMS = 2 };
 
 /* Plans the batch: the CUDA graph, and for the work-item schedules the work
- * list and per-grid dependency counters (device memory owned by the plan).
+ * list and its dependency counters (device memory owned by the plan).
  * dtype: GBS_F32 for every schedule, GBS_F64 for GBS_BATCH_STREAMS; a 3-D
  * grid or GBS_F64 under a work-item schedule is GBS_ERR_UNSUPPORTED. The
  * grids' buffers must stay valid while the plan is used. */
