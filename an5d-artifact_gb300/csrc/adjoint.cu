@@ -322,7 +322,6 @@ __global__ void __launch_bounds__(kAdjThreads) adj2d_kernel(const __grid_constan
   constexpr int NP = WANT_COEF ? NT : 1;
   constexpr int V = 16 / sizeof(T);
   constexpr int R = ST::kRad;
-  constexpr int W = 2 * R + 1;
   constexpr int SEG = 32 * V;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if ((int)blockIdx.x >= interior_blocks) {
