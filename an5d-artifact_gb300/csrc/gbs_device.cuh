@@ -204,16 +204,7 @@ template <> struct Arith<double> {
   static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
 };
 
-// acc = first ? c*a : acc + c*a   in the requested mode
-template <typename T, bool FMA>
-__device__ __forceinline__ T term(bool first, T acc, T c, T a) {
-  using A = Arith<T>;
-  if (first) return A::mul(c, a);
-  if constexpr (FMA) return A::fma(c, a, acc);
-  else return A::add(acc, A::mul(c, a));
-}
-template <typename T, bool FMA>
-__device__ __forceinline__ T term_first(T c, T a) { return Arith<T>::mul(c, a); }
+// acc + c*a in the requested mode (the first term of a sum is c*a alone)
 template <typename T, bool FMA>
 __device__ __forceinline__ T term_next(T acc, T c, T a) {
   using A = Arith<T>;
