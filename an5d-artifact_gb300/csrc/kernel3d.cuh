@@ -1,4 +1,7 @@
-// 3-D temporally-blocked stencil kernel family (sm_103a).
+// 3-D temporally-blocked stencil kernel family (sm_103a): the one-row-per-warp
+// kernel used for exact mode and for the boxes of more than 125 terms (FMA
+// mode otherwise runs the tensor-map tiles of kernel3d_tile.cuh), and the
+// launchers of both.
 //
 // Replaces the AN5D-generated 3-D kernels (e.g.
 // compiled/float/box3d1r-32x32-3-128_kernel.cu:4,284,509) and computes what

@@ -30,6 +30,13 @@
 // planes in flight, to which each arriving plane adds its terms.
 // Intermediate levels give their halo cells the fixed halo value, read from
 // HBM one step ahead.
+//
+// stencil3d_stream_kernel is the degree-1 form for double: one producer warp
+// more issues the tensor-map copies into the NS stages, each stage guarded by
+// a "full" mbarrier (the copy) and an "empty" one (one arrival per consumer
+// warp), so consumer warps run without a CTA barrier per plane; the FP64 pipe
+// bounds it, and a barrier left that pipe idle while the last warps of a
+// plane drained.
 #pragma once
 #include <cuda.h>
 
